@@ -1,0 +1,136 @@
+"""In-tree build of the native parts (no cmake, no pip install).
+
+  lib/libgpuothello2.so  CUDA kernels + C ABI (include/gpuothello2.h), sm_103a
+  bin/solver             C++ CLI `solver INPUT OUTPUT DEPTH` over the C ABI
+  bin/gen_boards         C++ board-file generator over the C ABI
+  oracle/lib/liboracle.so  CPU oracle (test infrastructure, not the product)
+  oracle/_ref/refsolve   the reference's own search built for the CPU, only
+                         where the reference sources are present (x86-64)
+
+Translation units are compiled in parallel; a unit is rebuilt only when a
+source it depends on (same directory headers included) is newer.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+HOST = os.path.join(PKG, "host")
+INCLUDE = os.path.join(ROOT, "include")
+LIB_DIR = os.path.join(PKG, "lib")
+BIN_DIR = os.path.join(PKG, "bin")
+OBJ_DIR = os.path.join(LIB_DIR, "obj")
+LIB = os.path.join(LIB_DIR, "libgpuothello2.so")
+SOLVER_BIN = os.path.join(BIN_DIR, "solver")
+GEN_BIN = os.path.join(BIN_DIR, "gen_boards")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "lib", "liboracle.so")
+REF_BIN = os.path.join(ORACLE_DIR, "_ref", "refsolve")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
+
+CU_SOURCES = ["plain.cu", "batched.cu", "prep.cu", "capi.cu"]
+INTPEAK_LIB = os.path.join(LIB_DIR, "libgpo_intpeak.so")
+
+
+def _headers(d):
+    return [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".cuh", ".h"))]
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _run(cmd, log=None):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        raise RuntimeError("build step failed: %s" % os.path.basename(cmd[-1]))
+    if log is not None:
+        log.append(r.stderr)
+    return r
+
+
+def build_library(verbose=False):
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    hdrs = _headers(CSRC) + [os.path.join(INCLUDE, "gpuothello2.h")]
+    objs, jobs = [], []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + hdrs + [__file__]):
+            jobs.append([NVCC] + NVCC_FLAGS + ["-c", s, "-o", o])
+    logs = []
+    if jobs:
+        with ThreadPoolExecutor(len(jobs)) as ex:
+            list(ex.map(lambda c: _run(c, logs), jobs))
+    if _stale(LIB, objs):
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    src = os.path.join(CSRC, "intpeak.cu")
+    if _stale(INTPEAK_LIB, [src, __file__]):
+        _run([NVCC] + NVCC_FLAGS + ["-shared", src, "-o", INTPEAK_LIB])
+    if verbose:
+        for lg in logs:
+            sys.stderr.write(lg)
+    return LIB
+
+
+def build_host():
+    os.makedirs(BIN_DIR, exist_ok=True)
+    cxx = shutil.which("g++") or "g++"
+    common = [os.path.join(HOST, "boardfile.cpp")]
+    deps = common + _headers(HOST) + [os.path.join(INCLUDE, "gpuothello2.h"), LIB]
+    flags = ["-std=c++17", "-O2", "-Wall", "-I", INCLUDE, "-I", HOST]
+    link = ["-L", LIB_DIR, "-lgpuothello2", "-Wl,-rpath,$ORIGIN/../lib", "-pthread"]
+    jobs = []
+    for main, out in (("solver_main.cpp", SOLVER_BIN), ("gen_main.cpp", GEN_BIN)):
+        src = os.path.join(HOST, main)
+        if _stale(out, [src] + deps):
+            jobs.append([cxx] + flags + [src] + common + ["-o", out] + link)
+    if jobs:
+        with ThreadPoolExecutor(len(jobs)) as ex:
+            list(ex.map(_run, jobs))
+    return SOLVER_BIN
+
+
+def build_oracle():
+    os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
+    src = os.path.join(ORACLE_DIR, "oracle.c")
+    if _stale(ORACLE_LIB, [src, os.path.join(ORACLE_DIR, "oracle.h")]):
+        _run(["gcc", "-O2", "-std=c11", "-Wall", "-shared", "-fPIC", "-pthread", src, "-o",
+              ORACLE_LIB])
+    return ORACLE_LIB
+
+
+def build_reference():
+    """The reference's search compiled for the CPU (oracle/ref_build.sh);
+    a no-op where the reference sources or an x86-64 host are absent."""
+    script = os.path.join(ORACLE_DIR, "ref_build.sh")
+    subprocess.run(["bash", script], check=True, capture_output=True)
+    return REF_BIN if os.path.exists(REF_BIN) else None
+
+
+def build_all(verbose=False):
+    with ThreadPoolExecutor(3) as ex:
+        f_lib = ex.submit(build_library, verbose)
+        f_orc = ex.submit(build_oracle)
+        f_ref = ex.submit(build_reference)
+        f_lib.result()
+        f_orc.result()
+        f_ref.result()
+    build_host()
+
+
+if __name__ == "__main__":
+    build_all(verbose="-v" in sys.argv)

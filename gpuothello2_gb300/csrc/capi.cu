@@ -1,0 +1,331 @@
+// C-ABI layer: library context, device buffers, the solve pipeline and
+// error mapping.  Replaces the reference's BatchedTask resource owner
+// (solver.cuh:8-25, solver.cu:313-348): instead of managed memory migrated
+// inside the timed region and a host busy-poll (main.cu:149-155), inputs are
+// copied explicitly into grow-only device buffers, the pipeline runs on one
+// stream, and the call waits on that stream.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/gpuothello2.h"
+#include "kernels.h"
+
+namespace gpo {
+namespace {
+
+struct Context {
+  int device = -1;
+  int sms = 0;
+  char name[256] = {0};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  size_t cap = 0;
+  u64* dP = nullptr;
+  u64* dO = nullptr;
+  signed char* dScore = nullptr;
+  signed char* dBest = nullptr;
+  unsigned long long* dNodes = nullptr;
+  unsigned* dPerm = nullptr;
+  unsigned* dHist = nullptr;    // 65 buckets
+  unsigned* dCursor = nullptr;  // 65 buckets
+  DeviceStats* dStats = nullptr;
+};
+
+std::mutex g_mutex;
+Context* g_ctx = nullptr;
+
+int cuda_fail(cudaError_t e, const char* what) {
+  std::fprintf(stderr, "gpuothello2: %s: %s (%s)\n", what, cudaGetErrorName(e), cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? GPO_ERR_NOMEM : GPO_ERR_CUDA;
+}
+
+#define GPO_CK(call)                                 \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+void free_buffers(Context* c) {
+  cudaFree(c->dP);
+  cudaFree(c->dO);
+  cudaFree(c->dScore);
+  cudaFree(c->dBest);
+  cudaFree(c->dNodes);
+  cudaFree(c->dPerm);
+  c->dP = c->dO = nullptr;
+  c->dScore = c->dBest = nullptr;
+  c->dNodes = nullptr;
+  c->dPerm = nullptr;
+  c->cap = 0;
+}
+
+int ensure_context(Context** out) {
+  if (!g_ctx) {
+    int dev = 0;
+    GPO_CK(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    GPO_CK(cudaGetDeviceProperties(&prop, dev));
+    Context* c = new Context();
+    c->device = dev;
+    c->sms = prop.multiProcessorCount;
+    std::snprintf(c->name, sizeof(c->name), "%s", prop.name);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&c->dHist, 65 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&c->dCursor, 65 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&c->dStats, sizeof(DeviceStats));
+    if (e != cudaSuccess) {
+      delete c;
+      return cuda_fail(e, "context setup");
+    }
+    g_ctx = c;
+  }
+  *out = g_ctx;
+  return GPO_OK;
+}
+
+int ensure_capacity(Context* c, size_t n) {
+  if (n <= c->cap) return GPO_OK;
+  free_buffers(c);
+  size_t cap = 1024;
+  while (cap < n) cap *= 2;
+  GPO_CK(cudaMalloc(&c->dP, cap * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->dO, cap * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->dScore, cap));
+  GPO_CK(cudaMalloc(&c->dBest, cap));
+  GPO_CK(cudaMalloc(&c->dNodes, cap * sizeof(unsigned long long)));
+  GPO_CK(cudaMalloc(&c->dPerm, cap * sizeof(unsigned)));
+  c->cap = cap;
+  return GPO_OK;
+}
+
+int status_to_error(unsigned st) {
+  if (st & kErrOverlap) return GPO_ERR_BOARD;
+  if (st & kErrDepth) return GPO_ERR_DEPTH;
+  if (st & kErrBudget) return GPO_ERR_TIMEOUT;
+  if (st & (kErrInternal | kErrTable)) return GPO_ERR_INTERNAL;
+  return GPO_OK;
+}
+
+int check_options(const gpo_options* opt) {
+  if (!opt) return GPO_OK;
+  if (opt->method != GPO_METHOD_BATCHED && opt->method != GPO_METHOD_PLAIN) return GPO_ERR_ARG;
+  if (opt->threads_per_block != 0 &&
+      (opt->threads_per_block < 32 || opt->threads_per_block > 1024 || opt->threads_per_block % 32))
+    return GPO_ERR_ARG;
+  return GPO_OK;
+}
+
+// Runs the solve pipeline on device arrays already in place.
+int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+              signed char* dBest, unsigned long long* dNodes, const gpo_options* opt,
+              gpo_stats* stats, cudaStream_t s) {
+  gpo_options o;
+  gpo_default_options(&o);
+  if (opt) o = *opt;
+  // ev0/ev1 bracket the search kernel only (kernel_ms)
+  GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
+  if (o.method == GPO_METHOD_PLAIN) {
+    GPO_CK(cudaEventRecord(c->ev0, s));
+    GPO_CK(launch_plain(dP, dO, n, depth, dScore, dNodes, c->dStats, s));
+  } else {
+    GPO_CK(cudaMemsetAsync(c->dHist, 0, 65 * sizeof(unsigned), s));
+    GPO_CK(launch_bucket(dP, dO, n, depth, c->dHist, c->dCursor, c->dPerm, c->dStats, c->sms, s));
+    GPO_CK(cudaEventRecord(c->ev0, s));
+    BatchedArgs a;
+    a.player = dP;
+    a.opp = dO;
+    a.perm = c->dPerm;
+    a.n = n;
+    a.depth = depth;
+    a.levels = batched_levels(depth);
+    a.ff = o.fastest_first_empties > 0 ? o.fastest_first_empties : 9;
+    a.score = dScore;
+    a.best = dBest;
+    a.nodes_out = dNodes;
+    a.stats = c->dStats;
+    a.node_budget = o.node_budget;
+    BatchedLaunch cfg;
+    cfg.threads = o.threads_per_block > 0 ? o.threads_per_block : 128;
+    cfg.smem_stack = true;
+    GPO_CK(launch_batched(a, cfg, c->sms, s));
+  }
+  GPO_CK(cudaEventRecord(c->ev1, s));
+  DeviceStats hs;
+  GPO_CK(cudaMemcpyAsync(&hs, c->dStats, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->nodes = hs.nodes;
+    stats->table_probes = hs.tt_probes;
+    stats->table_hits = hs.tt_hits;
+    stats->table_updates = hs.tt_updates;
+    stats->learned_calls = hs.learned_calls;
+    stats->kernel_ms = ms;
+  }
+  return status_to_error(hs.status);
+}
+
+int validate_call(const void* a, const void* b, const void* out, int n, int depth) {
+  if (n < 0) return GPO_ERR_ARG;
+  if (n > 0 && (!a || !b || !out)) return GPO_ERR_ARG;
+  if (depth < 1 || depth > kMaxEmpties) return GPO_ERR_DEPTH;
+  return GPO_OK;
+}
+
+}  // namespace
+}  // namespace gpo
+
+using namespace gpo;
+
+extern "C" {
+
+void gpo_default_options(gpo_options* opt) {
+  if (!opt) return;
+  std::memset(opt, 0, sizeof(*opt));
+  opt->method = GPO_METHOD_BATCHED;
+  opt->use_table = -1;
+  opt->use_learned = -1;
+}
+
+int solve_batch_ex(const uint64_t* player, const uint64_t* opp, int n, int depth, int8_t* score,
+                   int8_t* best_move, uint64_t* nodes, const gpo_options* opt, gpo_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = validate_call(player, opp, score, n, depth);
+  if (rc == GPO_OK) rc = check_options(opt);
+  if (rc != GPO_OK) return rc;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (n == 0) return GPO_OK;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Context* c = nullptr;
+  if ((rc = ensure_context(&c)) != GPO_OK) return rc;
+  if ((rc = ensure_capacity(c, static_cast<size_t>(n))) != GPO_OK) return rc;
+  cudaStream_t s = c->stream;
+  GPO_CK(cudaMemcpyAsync(c->dP, player, n * sizeof(u64), cudaMemcpyHostToDevice, s));
+  GPO_CK(cudaMemcpyAsync(c->dO, opp, n * sizeof(u64), cudaMemcpyHostToDevice, s));
+  rc = run_solve(c, c->dP, c->dO, n, depth, c->dScore, best_move ? c->dBest : nullptr,
+                 nodes ? c->dNodes : nullptr, opt, stats, s);
+  if (rc == GPO_ERR_CUDA || rc == GPO_ERR_NOMEM) return rc;
+  GPO_CK(cudaMemcpyAsync(score, c->dScore, n, cudaMemcpyDeviceToHost, s));
+  if (best_move) GPO_CK(cudaMemcpyAsync(best_move, c->dBest, n, cudaMemcpyDeviceToHost, s));
+  if (nodes)
+    GPO_CK(cudaMemcpyAsync(nodes, c->dNodes, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  if (stats)
+    stats->total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+int solve_batch(const uint64_t* player, const uint64_t* opp, int n, int depth, int8_t* score) {
+  return solve_batch_ex(player, opp, n, depth, score, nullptr, nullptr, nullptr, nullptr);
+}
+
+int solve_batch_device(const uint64_t* d_player, const uint64_t* d_opp, int n, int depth,
+                       int8_t* d_score, int8_t* d_best_move, uint64_t* d_nodes,
+                       const gpo_options* opt, gpo_stats* stats, void* stream) {
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = validate_call(d_player, d_opp, d_score, n, depth);
+  if (rc == GPO_OK) rc = check_options(opt);
+  if (rc != GPO_OK) return rc;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (n == 0) return GPO_OK;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Context* c = nullptr;
+  if ((rc = ensure_context(&c)) != GPO_OK) return rc;
+  if ((rc = ensure_capacity(c, static_cast<size_t>(n))) != GPO_OK) return rc;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  rc = run_solve(c, reinterpret_cast<const u64*>(d_player), reinterpret_cast<const u64*>(d_opp), n,
+                 depth, reinterpret_cast<signed char*>(d_score),
+                 reinterpret_cast<signed char*>(d_best_move),
+                 reinterpret_cast<unsigned long long*>(d_nodes), opt, stats, s);
+  if (stats)
+    stats->total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+int gpo_generate_device(uint64_t seed, uint64_t first, int n, int min_empties, int max_empties,
+                        uint64_t* d_player, uint64_t* d_opp, void* stream) {
+  if (n < 0 || (n > 0 && (!d_player || !d_opp))) return GPO_ERR_ARG;
+  if (min_empties < 0 || max_empties > 60 || min_empties > max_empties) return GPO_ERR_ARG;
+  if (seed >= (1ULL << 32)) return GPO_ERR_ARG;
+  if (n == 0) return GPO_OK;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Context* c = nullptr;
+  int rc = ensure_context(&c);
+  if (rc != GPO_OK) return rc;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  GPO_CK(launch_generate(seed, first, n, min_empties, max_empties,
+                         reinterpret_cast<u64*>(d_player), reinterpret_cast<u64*>(d_opp), s));
+  GPO_CK(cudaStreamSynchronize(s));
+  return GPO_OK;
+}
+
+int gpo_generate(uint64_t seed, uint64_t first, int n, int min_empties, int max_empties,
+                 uint64_t* player, uint64_t* opp) {
+  if (n < 0 || (n > 0 && (!player || !opp))) return GPO_ERR_ARG;
+  if (min_empties < 0 || max_empties > 60 || min_empties > max_empties) return GPO_ERR_ARG;
+  if (seed >= (1ULL << 32)) return GPO_ERR_ARG;
+  if (n == 0) return GPO_OK;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Context* c = nullptr;
+  int rc = ensure_context(&c);
+  if (rc != GPO_OK) return rc;
+  if ((rc = ensure_capacity(c, static_cast<size_t>(n))) != GPO_OK) return rc;
+  cudaStream_t s = c->stream;
+  GPO_CK(launch_generate(seed, first, n, min_empties, max_empties, c->dP, c->dO, s));
+  GPO_CK(cudaMemcpyAsync(player, c->dP, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaMemcpyAsync(opp, c->dO, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  return GPO_OK;
+}
+
+void solve_shutdown(void) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_ctx) return;
+  Context* c = g_ctx;
+  cudaStreamSynchronize(c->stream);
+  free_buffers(c);
+  cudaFree(c->dHist);
+  cudaFree(c->dCursor);
+  cudaFree(c->dStats);
+  cudaEventDestroy(c->ev0);
+  cudaEventDestroy(c->ev1);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  g_ctx = nullptr;
+}
+
+const char* gpo_strerror(int status) {
+  switch (status) {
+    case GPO_OK: return "ok";
+    case GPO_ERR_ARG: return "invalid argument";
+    case GPO_ERR_DEPTH: return "depth out of range or a position has more empty squares than depth";
+    case GPO_ERR_BOARD: return "a square is occupied by both sides";
+    case GPO_ERR_CUDA: return "CUDA runtime error";
+    case GPO_ERR_NOMEM: return "out of memory";
+    case GPO_ERR_TIMEOUT: return "node budget exceeded";
+    case GPO_ERR_INTERNAL: return "internal consistency check failed";
+    case GPO_ERR_IO: return "file I/O error";
+    default: return "unknown status";
+  }
+}
+
+int gpo_device_info(char* name, int name_len, int* sm_count) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Context* c = nullptr;
+  const int rc = ensure_context(&c);
+  if (rc != GPO_OK) return rc;
+  if (name && name_len > 0) std::snprintf(name, static_cast<size_t>(name_len), "%s", c->name);
+  if (sm_count) *sm_count = c->sms;
+  return GPO_OK;
+}
+
+}  // extern "C"

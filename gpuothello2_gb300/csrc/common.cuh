@@ -1,0 +1,51 @@
+// Shared definitions for the solver kernels and the C-ABI layer.
+#pragma once
+#include <cstdint>
+
+#include "bitboard.cuh"
+
+namespace gpo {
+
+// Largest empty count a position may have (stack sizing).  Every kernel
+// rejects a position with more empties than the call's depth, and the
+// C-ABI rejects depth > GPO_MAX_EMPTIES.
+constexpr int kMaxEmpties = 32;
+
+constexpr u64 kCorners = 0x8100000000000081ULL;
+
+// Best-move codes (the reference's hand::PASS / hand::NOMOVE, alphabeta.cuh:7-10).
+constexpr int kMovePassDev = 64;
+constexpr int kMoveNoneDev = 65;
+
+// Error bits set by kernels in the device status word (host maps them to
+// the negative GPO_ERR_* codes of the C-ABI).
+enum : unsigned int {
+  kErrDepth = 1u << 0,     // a position has more empties than `depth`
+  kErrOverlap = 1u << 1,   // a square is set in both bitboards
+  kErrBudget = 1u << 2,    // a search hit the per-position node budget
+  kErrTable = 1u << 3,     // a table update gave up after its retry limit
+  kErrInternal = 1u << 4,  // stack index out of range (never expected)
+};
+
+// Per-launch device counters (one instance in device memory per context).
+struct DeviceStats {
+  unsigned long long nodes;
+  unsigned long long tt_probes;
+  unsigned long long tt_hits;
+  unsigned long long tt_updates;
+  unsigned long long learned_calls;
+  unsigned int status;
+  unsigned int next;  // work-queue cursor of the persistent kernel
+};
+
+__device__ __forceinline__ int ctz64(u64 x) { return __ffsll(static_cast<long long>(x)) - 1; }
+
+// Warp-level sum of a 64-bit counter, one atomic per warp.  Must be called
+// by all 32 lanes of the warp together (kernels call it after their loops,
+// where every lane has arrived).
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+}  // namespace gpo

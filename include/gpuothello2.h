@@ -1,0 +1,136 @@
+/*
+ * gpuothello2.h -- C ABI of the GB300 batched exact Othello endgame solver.
+ *
+ * The reference drives its GPU solver through a C++ class, BatchedTask
+ * (solver.cuh:8-25; solver.cu:313-348): construct with (batch_size,
+ * max_depth, Table&), fill `abp[]` = AlphaBetaProblem{player, opponent}
+ * (alphabeta.cuh:13-21) in managed memory, launch(), poll is_ready(), read
+ * `result[]` (int32) -- with the CLI's solve() doing exactly that
+ * (main.cu:123-173).  This header replaces that class with plain functions
+ * over caller-owned host (or device) arrays, so any language with a C FFI can
+ * bind it.  See INTEGRATION.md for the bindings.
+ *
+ * Conventions
+ *   - A position is two disjoint 64-bit bitboards: `player` = discs of the
+ *     side to move, `opp` = discs of the other side; square = row*8 + col,
+ *     A1 = bit 0 (main.cu:31-39).
+ *   - Scores are exact final disc differences from the side to move, with
+ *     the empty squares awarded to the winner (board.cuh:7-18): even
+ *     integers in [-64, 64].
+ *   - `depth` is the reference's DEPTH: the largest number of empty squares
+ *     any position of the batch may have (README.md:56-58).  A position with
+ *     more empties than `depth` is an error, not undefined behaviour.
+ *   - All calls are synchronous and serialised by an internal lock; device
+ *     buffers, the stream and the transposition table live in a library
+ *     context created on first use on the current CUDA device and released
+ *     by solve_shutdown().
+ *   - Every entry point returns GPO_OK (0) or a negative GPO_ERR_* status.
+ */
+#ifndef GPUOTHELLO2_H
+#define GPUOTHELLO2_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPO_OK 0
+#define GPO_ERR_ARG (-1)      /* null pointer, n < 0, bad option value */
+#define GPO_ERR_DEPTH (-2)    /* depth out of [1, 32] or a position has more empties than depth */
+#define GPO_ERR_BOARD (-3)    /* a square is set in both bitboards */
+#define GPO_ERR_CUDA (-4)     /* CUDA runtime error (no device, launch failure, ...) */
+#define GPO_ERR_NOMEM (-5)    /* device or pinned-host allocation failed */
+#define GPO_ERR_TIMEOUT (-6)  /* a search exceeded gpo_options.node_budget */
+#define GPO_ERR_INTERNAL (-7) /* a kernel consistency check failed */
+#define GPO_ERR_IO (-8)       /* file could not be read or written */
+
+/* Move codes in best-move outputs: 0..63 = square, 64 = pass, 65 = no move
+ * (game over) -- the reference's hand::PASS / hand::NOMOVE (alphabeta.cuh:7-10). */
+#define GPO_MOVE_PASS 64
+#define GPO_MOVE_NONE 65
+
+/* Search methods. */
+#define GPO_METHOD_BATCHED 0 /* persistent, empties-bucketed kernel (default) */
+#define GPO_METHOD_PLAIN 1   /* thread-per-board kernel, the reference's exact tree */
+
+typedef struct gpo_options {
+  int method;                 /* GPO_METHOD_* */
+  int use_table;              /* transposition table: -1 auto, 0 off, 1 on */
+  int use_learned;            /* learned move ordering: -1 auto, 0 off, 1 on */
+  int threads_per_block;      /* 0 = tuned default */
+  int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties; 0 = tuned */
+  int learned_min_empties;    /* learned ordering at nodes with >= this many empties; 0 = 14 */
+  uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog) */
+} gpo_options;
+
+typedef struct gpo_stats {
+  uint64_t nodes;         /* positions visited (root, children, pass frames) */
+  uint64_t table_probes;  /* transposition-table lookups */
+  uint64_t table_hits;    /* lookups that found the position */
+  uint64_t table_updates; /* stores into the table */
+  uint64_t learned_calls; /* learned-orderer evaluations */
+  double kernel_ms;       /* device time of the search kernels (CUDA events) */
+  double total_ms;        /* wall time of the call */
+} gpo_stats;
+
+/* Fills *opt with the defaults (all fields "auto"/0). */
+void gpo_default_options(gpo_options* opt);
+
+/*
+ * Exact-solves n positions.  player/opp/score are caller-owned host arrays
+ * of n elements; score[i] receives the exact score of position i.
+ * Replaces BatchedTask ctor + abp fill + launch + is_ready polling + result
+ * read-back (solver.cuh:8-25, solver.cu:313-348, main.cu:135-171).
+ */
+int solve_batch(const uint64_t* player, const uint64_t* opp, int n, int depth, int8_t* score);
+
+/*
+ * As solve_batch, with options (NULL = defaults), an optional best-move
+ * output (NULL = not wanted; 0..63, GPO_MOVE_PASS or GPO_MOVE_NONE), an
+ * optional per-position node count output (NULL = not wanted) and optional
+ * statistics (NULL = not wanted).  The table counters of gpo_stats are the
+ * reference's "table update count / hit / find" (table.cuh:26-40,
+ * main.cu:158-162).
+ */
+int solve_batch_ex(const uint64_t* player, const uint64_t* opp, int n, int depth, int8_t* score,
+                   int8_t* best_move, uint64_t* nodes, const gpo_options* opt, gpo_stats* stats);
+
+/*
+ * As solve_batch_ex, but every array is a device pointer on the current
+ * device and the work is ordered on `stream` (a cudaStream_t; NULL = the
+ * library's own stream).  Returns after the work completes.
+ */
+int solve_batch_device(const uint64_t* d_player, const uint64_t* d_opp, int n, int depth,
+                       int8_t* d_score, int8_t* d_best_move, uint64_t* d_nodes,
+                       const gpo_options* opt, gpo_stats* stats, void* stream);
+
+/*
+ * Generates n positions of the seeded random-playout stream `seed`, indices
+ * first .. first+n-1, on the GPU (host output arrays).  Empty count is
+ * min_empties when min == max, else uniform in [min_empties, max_empties].
+ * Definition: xoshiro256** seeded with four successive splitmix64 outputs
+ * from x0 = (seed << 32) + index; uniform(k) = high 64 bits of next() * k;
+ * the empty count (if ranged) is drawn first; from the standard start
+ * (black to move, black d5/e4, white d4/e5) play the uniform(k)-th set bit
+ * of the k legal moves (from bit 0), pass when only the other side can move,
+ * restart the game (same PRNG stream) if it ends early, and stop when exactly
+ * the wanted number of squares is empty.
+ */
+int gpo_generate(uint64_t seed, uint64_t first, int n, int min_empties, int max_empties,
+                 uint64_t* player, uint64_t* opp);
+int gpo_generate_device(uint64_t seed, uint64_t first, int n, int min_empties, int max_empties,
+                        uint64_t* d_player, uint64_t* d_opp, void* stream);
+
+/* Releases the library context (device buffers, table, stream). */
+void solve_shutdown(void);
+
+/* Human-readable text for a status code. */
+const char* gpo_strerror(int status);
+
+/* Name of the device the context runs on, and its SM count (0 if none). */
+int gpo_device_info(char* name, int name_len, int* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUOTHELLO2_H */

@@ -1,0 +1,91 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports
+every function include/gpuothello2.h declares, argument validation, and the
+CLI's argument and file errors (main.cu:175-185, 49-67 semantics)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN, ROOT
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "gpuothello2.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*([a-z_0-9]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(built):
+    import gpuothello2_gb300 as g
+
+    names = declared_functions()
+    assert len(names) >= 9
+    lib = ctypes.CDLL(built.LIB)
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(g.EXPORTED_SYMBOLS)
+
+
+def test_argument_validation_needs_no_device(built):
+    import gpuothello2_gb300 as g
+
+    L = g.lib()
+    p = np.zeros(4, np.uint64)
+    s = np.zeros(4, np.int8)
+    assert L.solve_batch(p.ctypes.data, p.ctypes.data, -1, 10, s.ctypes.data) == g.GPO_ERR_ARG
+    assert L.solve_batch(None, p.ctypes.data, 4, 10, s.ctypes.data) == g.GPO_ERR_ARG
+    assert L.solve_batch(p.ctypes.data, p.ctypes.data, 4, 0, s.ctypes.data) == g.GPO_ERR_DEPTH
+    assert L.solve_batch(p.ctypes.data, p.ctypes.data, 4, 33, s.ctypes.data) == g.GPO_ERR_DEPTH
+    assert L.solve_batch(p.ctypes.data, p.ctypes.data, 0, 10, s.ctypes.data) == g.GPO_OK
+    bad = g.options(method=7)
+    assert L.solve_batch_ex(p.ctypes.data, p.ctypes.data, 4, 10, s.ctypes.data, None, None,
+                            ctypes.byref(bad), None) == g.GPO_ERR_ARG
+    assert L.gpo_generate(0, 0, 4, 10, 61, p.ctypes.data, p.ctypes.data) == g.GPO_ERR_ARG
+    assert L.gpo_generate(1 << 40, 0, 4, 10, 10, p.ctypes.data, p.ctypes.data) == g.GPO_ERR_ARG
+    assert g.strerror(g.GPO_ERR_DEPTH).startswith("depth")
+
+
+def run_cli(args, cwd=None):
+    from gpuothello2_gb300 import build
+
+    return subprocess.run([build.SOLVER_BIN] + args, capture_output=True, text=True, cwd=cwd,
+                          timeout=120)
+
+
+def test_cli_usage_and_think_mode(built):
+    r = run_cli([])
+    assert r.returncode == 1 and "usage:" in r.stderr
+    r = run_cli(["a", "b", "10", "3"])
+    assert r.returncode == 2 and "think mode" in r.stderr
+    r = run_cli(["a", "b", "x"])
+    assert r.returncode == 1
+
+
+def test_cli_file_errors(built, tmp_path):
+    r = run_cli([str(tmp_path / "missing.txt"), str(tmp_path / "o.txt"), "10"])
+    assert r.returncode != 0 and "cannot open" in r.stderr
+    short = tmp_path / "short.txt"
+    short.write_text("3\n!!%[nNNNNNnNNNNN\n")
+    r = run_cli([str(short), str(tmp_path / "o.txt"), "10"])
+    assert r.returncode != 0 and "Failed to load boards" in r.stderr
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1\n!!%[nNNN NnNNNNN\n")
+    r = run_cli([str(bad), str(tmp_path / "o.txt"), "10"])
+    assert r.returncode != 0 and "bad board" in r.stderr
+    trunc = tmp_path / "trunc.txt"
+    trunc.write_text("1\n!!%[nNNNN\n")
+    r = run_cli([str(trunc), str(tmp_path / "o.txt"), "10"])
+    assert r.returncode != 0 and "bad board" in r.stderr
+
+
+def test_python_board_file_roundtrip(tmp_path):
+    from gpuothello2_gb300 import codec
+
+    p, o = codec.read_board_file(os.path.join(GOLDEN, "c1_seed0_e10.txt"))
+    path = tmp_path / "b.txt"
+    codec.write_board_file(str(path), p, o)
+    assert path.read_text() == open(os.path.join(GOLDEN, "c1_seed0_e10.txt")).read()

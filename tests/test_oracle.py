@@ -1,0 +1,138 @@
+"""The CPU oracle pinned against the reference's own outputs (tests/golden/,
+produced by the reference's search code -- see make_golden.py there)."""
+import os
+
+import numpy as np
+import pytest
+
+from gpuothello2_gb300 import codec
+from tests.conftest import GOLDEN
+
+FIXTURES = [
+    # name, seed, count, lo, hi, depth
+    ("c1_seed0_e10", 0, 4096, 10, 10, 10),
+    ("c3_seed2_mixed", 2, 256, 8, 16, 16),
+    ("c4_seed4_e18", 4, 16, 18, 18, 18),
+    ("c5_seed5_e20_22", 5, 4, 20, 22, 22),
+]
+
+
+def golden_ref(name):
+    path = os.path.join(GOLDEN, name + ".ref")
+    if not os.path.exists(path):
+        pytest.skip("fixture %s not generated" % name)
+    boards, scores, steps = [], [], []
+    with open(path) as f:
+        for ln in f:
+            s, sc, st = ln.split()
+            boards.append(codec.decode(s))
+            scores.append(int(sc))
+            steps.append(int(st))
+    p = np.array([b[0] for b in boards], np.uint64)
+    o = np.array([b[1] for b in boards], np.uint64)
+    return p, o, np.array(scores), np.array(steps, np.uint64)
+
+
+def test_flip_and_mobility_match_naive(oracle):
+    rng = np.random.default_rng(1)
+    L = oracle.L
+    bad = 0
+    for _ in range(3000):
+        x = int(rng.integers(0, 2**64, dtype=np.uint64))
+        y = int(rng.integers(0, 2**64, dtype=np.uint64))
+        p, o = x & y, x & ~y & (2**64 - 1)
+        bad += L.orc_mobility(p, o) != L.orc_mobility_naive(p, o)
+        for sq in range(64):
+            if not ((p | o) >> sq) & 1:
+                bad += L.orc_flip(p, o, sq) != L.orc_flip_naive(p, o, sq)
+    assert bad == 0
+
+
+def test_final_score_rule(oracle):
+    # empties go to the winner (board.cuh:7-18)
+    L = oracle.L
+    assert L.orc_final_score(0b111, 0b1) == 64 - 2
+    assert L.orc_final_score(0b1, 0b111) == 2 - 64
+    assert L.orc_final_score(0b11, 0b1100) == 0
+    assert L.orc_final_score(0, 0) == 0
+    assert L.orc_final_score(2**64 - 1, 0) == 64
+
+
+@pytest.mark.parametrize("name,seed,count,lo,hi,depth", FIXTURES)
+def test_generator_reproduces_golden_boards(oracle, name, seed, count, lo, hi, depth):
+    path = os.path.join(GOLDEN, name + ".txt")
+    if not os.path.exists(path):
+        pytest.skip("fixture missing")
+    gp, go = codec.read_board_file(path)
+    p, o = oracle.generate(seed, count, lo, hi)
+    assert np.array_equal(p, gp) and np.array_equal(o, go)
+    e = codec.empties(p, o)
+    assert e.min() >= lo and e.max() <= hi
+
+
+@pytest.mark.parametrize("name,seed,count,lo,hi,depth", FIXTURES)
+def test_oracle_reference_tree_matches_reference(oracle, name, seed, count, lo, hi, depth):
+    """Scores AND per-position loop-step counts equal the reference's: the
+    oracle walks the reference's exact tree."""
+    p, o, scores, steps = golden_ref(name)
+    if name.startswith("c5"):
+        pytest.skip("20-22 empties in reference order take minutes on the CPU; covered by the fast solver")
+    sc, st, _, _ = oracle.solve_batch(p, o, depth, mode=0)
+    assert np.array_equal(sc.astype(int), scores)
+    assert np.array_equal(st, steps)
+
+
+@pytest.mark.parametrize("name,seed,count,lo,hi,depth", FIXTURES)
+def test_oracle_fast_solver_matches_reference(oracle, name, seed, count, lo, hi, depth):
+    p, o, scores, _ = golden_ref(name)
+    sc, _, _, best = oracle.solve_batch(p, o, depth, mode=1)
+    assert np.array_equal(sc.astype(int), scores)
+
+
+def test_readme_boards(oracle):
+    p, o, scores, steps = golden_ref("readme9")
+    sc, st, _, _ = oracle.solve_batch(p, o, 10, mode=0)
+    assert np.array_equal(sc.astype(int), scores)
+    assert np.array_equal(st, steps)
+    # README.md:11 decodes to this position (checked by hand against the
+    # reference's SIMD decoder)
+    assert codec.decode("!!%[nNNNNNnNNNNN") == (0xfffff7fffff78300, 0x0000080000087000)
+
+
+def test_codec_matches_reference_vectors(oracle):
+    path = os.path.join(GOLDEN, "codec_vectors.txt")
+    n = 0
+    with open(path, encoding="latin-1") as f:
+        for ln in f:
+            ph, oh, s = ln.rstrip("\n").split(" ", 2)
+            p, o = int(ph, 16), int(oh, 16)
+            assert oracle.encode(p, o) == s
+            assert codec.encode(p, o) == s
+            assert oracle.decode(s) == (p, o)
+            assert codec.decode(s) == (p, o)
+            n += 1
+    assert n == 2000
+
+
+def test_codec_rejects_bad_chars(oracle):
+    with pytest.raises(ValueError):
+        codec.decode("!!!!!!!!!!!!!!! ")
+    with pytest.raises(ValueError):
+        codec.decode("short")
+    with pytest.raises(ValueError):
+        oracle.decode("~" * 16)
+
+
+def test_best_move_is_optimal(oracle):
+    """The fast solver's best move reaches the root value."""
+    p, o = oracle.generate(3, 64, 12, 14)
+    sc, _, _, best = oracle.solve_batch(p, o, 32, mode=1)
+    for i in range(len(p)):
+        b = int(best[i])
+        if b >= 64:
+            continue
+        f = oracle.L.orc_flip(int(p[i]), int(o[i]), b)
+        assert f != 0
+        cp, co = int(o[i]) ^ f, int(p[i]) ^ f ^ (1 << b)
+        v, _, _, _ = oracle.solve_batch(np.array([cp], np.uint64), np.array([co], np.uint64), 32, mode=1)
+        assert -int(v[0]) == int(sc[i])
