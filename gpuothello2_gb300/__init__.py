@@ -43,6 +43,8 @@ class Options(ctypes.Structure):
         ("fastest_first_empties", ctypes.c_int),
         ("learned_min_empties", ctypes.c_int),
         ("node_budget", ctypes.c_uint64),
+        ("split_min_empties", ctypes.c_int),
+        ("wait_limit_ms", ctypes.c_int),
     ]
 
 
@@ -53,6 +55,7 @@ class Stats(ctypes.Structure):
         ("table_hits", ctypes.c_uint64),
         ("table_updates", ctypes.c_uint64),
         ("learned_calls", ctypes.c_uint64),
+        ("splits", ctypes.c_uint64),
         ("kernel_ms", ctypes.c_double),
         ("total_ms", ctypes.c_double),
     ]

@@ -33,7 +33,21 @@ struct Context {
   unsigned* dHist = nullptr;    // 65 buckets
   unsigned* dCursor = nullptr;  // 65 buckets
   DeviceStats* dStats = nullptr;
+  unsigned char* dFrames = nullptr;  // batched kernel's global frame slots
+  size_t frames_cap = 0;
+  // work donation: accumulators for n + task_cap slots, queue of task_cap
+  unsigned task_cap = 0;
+  size_t slot_cap = 0;
+  unsigned* dAcc = nullptr;
+  unsigned* dPending = nullptr;
+  unsigned* dParent = nullptr;
+  unsigned char* dPsq = nullptr;
+  unsigned* dTop = nullptr;
+  DonatedTask* dQueue = nullptr;
+  unsigned* dReady = nullptr;
 };
+
+constexpr unsigned kTaskCap = 1u << 22;  // donated subtrees per call
 
 std::mutex g_mutex;
 Context* g_ctx = nullptr;
@@ -49,7 +63,42 @@ int cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
   } while (0)
 
+void free_donation(Context* c) {
+  cudaFree(c->dAcc);
+  cudaFree(c->dPending);
+  cudaFree(c->dParent);
+  cudaFree(c->dPsq);
+  cudaFree(c->dTop);
+  cudaFree(c->dQueue);
+  cudaFree(c->dReady);
+  c->dAcc = c->dPending = c->dParent = c->dTop = c->dReady = nullptr;
+  c->dPsq = nullptr;
+  c->dQueue = nullptr;
+  c->task_cap = 0;
+  c->slot_cap = 0;
+}
+
+int ensure_donation(Context* c, size_t n) {
+  const size_t slots = n + kTaskCap;
+  if (c->task_cap == kTaskCap && c->slot_cap >= slots) return GPO_OK;
+  free_donation(c);
+  GPO_CK(cudaMalloc(&c->dAcc, slots * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dPending, slots * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dParent, kTaskCap * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dPsq, kTaskCap));
+  GPO_CK(cudaMalloc(&c->dTop, kTaskCap * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dQueue, kTaskCap * sizeof(DonatedTask)));
+  GPO_CK(cudaMalloc(&c->dReady, kTaskCap * sizeof(unsigned)));
+  c->task_cap = kTaskCap;
+  c->slot_cap = slots;
+  return GPO_OK;
+}
+
 void free_buffers(Context* c) {
+  free_donation(c);
+  cudaFree(c->dFrames);
+  c->dFrames = nullptr;
+  c->frames_cap = 0;
   cudaFree(c->dP);
   cudaFree(c->dO);
   cudaFree(c->dScore);
@@ -107,7 +156,7 @@ int ensure_capacity(Context* c, size_t n) {
 int status_to_error(unsigned st) {
   if (st & kErrOverlap) return GPO_ERR_BOARD;
   if (st & kErrDepth) return GPO_ERR_DEPTH;
-  if (st & kErrBudget) return GPO_ERR_TIMEOUT;
+  if (st & (kErrBudget | kErrWait)) return GPO_ERR_TIMEOUT;
   if (st & (kErrInternal | kErrTable)) return GPO_ERR_INTERNAL;
   return GPO_OK;
 }
@@ -143,7 +192,6 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
     a.perm = c->dPerm;
     a.n = n;
     a.depth = depth;
-    a.levels = batched_levels(depth);
     a.ff = o.fastest_first_empties > 0 ? o.fastest_first_empties : 9;
     a.score = dScore;
     a.best = dBest;
@@ -152,7 +200,35 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
     a.node_budget = o.node_budget;
     BatchedLaunch cfg;
     cfg.threads = o.threads_per_block > 0 ? o.threads_per_block : 128;
-    cfg.smem_stack = true;
+    GPO_CK(batched_plan(cfg.threads, depth, &a.smem_top));
+    cfg.grid = 0;
+    size_t smem = 0;
+    GPO_CK(batched_grid(cfg.threads, a.smem_top, c->sms, &cfg.grid, &smem));
+    const size_t need = static_cast<size_t>(depth > a.smem_top ? depth - a.smem_top : 0) *
+                        static_cast<size_t>(cfg.grid) * cfg.threads * 20;
+    if (need > c->frames_cap) {
+      cudaFree(c->dFrames);
+      c->dFrames = nullptr;
+      c->frames_cap = 0;
+      GPO_CK(cudaMalloc(&c->dFrames, need));
+      c->frames_cap = need;
+    }
+    a.gframes = c->dFrames;
+    const int rcd = ensure_donation(c, static_cast<size_t>(n));
+    if (rcd != GPO_OK) return rcd;
+    a.donate_min = o.split_min_empties < 0 ? 0 : (o.split_min_empties > 0 ? o.split_min_empties : 10);
+    a.task_cap = c->task_cap;
+    a.acc = c->dAcc;
+    a.pending = c->dPending;
+    a.parent = c->dParent;
+    a.psq = c->dPsq;
+    a.top = c->dTop;
+    a.queue = c->dQueue;
+    a.ready = c->dReady;
+    a.wait_limit_ns = static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 120000) *
+                      1000000ULL;
+    GPO_CK(cudaMemsetAsync(c->dReady, 0, static_cast<size_t>(c->task_cap) * sizeof(unsigned), s));
+    if (dNodes) GPO_CK(cudaMemsetAsync(dNodes, 0, static_cast<size_t>(n) * sizeof(u64), s));
     GPO_CK(launch_batched(a, cfg, c->sms, s));
   }
   GPO_CK(cudaEventRecord(c->ev1, s));
@@ -167,6 +243,7 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
     stats->table_hits = hs.tt_hits;
     stats->table_updates = hs.tt_updates;
     stats->learned_calls = hs.learned_calls;
+    stats->splits = hs.donations;
     stats->kernel_ms = ms;
   }
   return status_to_error(hs.status);

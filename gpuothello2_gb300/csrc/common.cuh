@@ -25,6 +25,7 @@ enum : unsigned int {
   kErrBudget = 1u << 2,    // a search hit the per-position node budget
   kErrTable = 1u << 3,     // a table update gave up after its retry limit
   kErrInternal = 1u << 4,  // stack index out of range (never expected)
+  kErrWait = 1u << 5,      // an idle lane waited longer than the wait limit
 };
 
 // Per-launch device counters (one instance in device memory per context).
@@ -35,7 +36,12 @@ struct DeviceStats {
   unsigned long long tt_updates;
   unsigned long long learned_calls;
   unsigned int status;
-  unsigned int next;  // work-queue cursor of the persistent kernel
+  unsigned int next;         // work-queue cursor of the persistent kernel
+  unsigned int done;         // input positions finished
+  unsigned int dq_head;      // donation queue: records reserved by idle lanes
+  unsigned int dq_tail;      // donation queue: records written by donors
+  unsigned int task_count;   // donated task slots handed out
+  unsigned long long donations;
 };
 
 __device__ __forceinline__ int ctz64(u64 x) { return __ffsll(static_cast<long long>(x)) - 1; }

@@ -8,7 +8,7 @@
  * `result[]` (int32) -- with the CLI's solve() doing exactly that
  * (main.cu:123-173).  This header replaces that class with plain functions
  * over caller-owned host (or device) arrays, so any language with a C FFI can
- * bind it.  See INTEGRATION.md for the bindings.
+ * bind it.
  *
  * Conventions
  *   - A position is two disjoint 64-bit bitboards: `player` = discs of the
@@ -61,6 +61,9 @@ typedef struct gpo_options {
   int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties; 0 = tuned */
   int learned_min_empties;    /* learned ordering at nodes with >= this many empties; 0 = 14 */
   uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog) */
+  int split_min_empties;      /* hard positions are split across lanes from this many
+                                 empties; 0 = tuned default, negative = never split */
+  int wait_limit_ms;          /* bound on an idle lane's wait for split work; 0 = 120000 */
 } gpo_options;
 
 typedef struct gpo_stats {
@@ -69,6 +72,7 @@ typedef struct gpo_stats {
   uint64_t table_hits;    /* lookups that found the position */
   uint64_t table_updates; /* stores into the table */
   uint64_t learned_calls; /* learned-orderer evaluations */
+  uint64_t splits;        /* subtrees handed to other lanes */
   double kernel_ms;       /* device time of the search kernels (CUDA events) */
   double total_ms;        /* wall time of the call */
 } gpo_stats;
