@@ -30,7 +30,8 @@ METHOD_PLAIN = 1
 EXPORTED_SYMBOLS = (
     "gpo_default_options", "solve_batch", "solve_batch_ex", "solve_batch_device",
     "gpo_generate", "gpo_generate_device", "solve_shutdown", "gpo_strerror",
-    "gpo_device_info",
+    "gpo_device_info", "gpo_mlp_param_count", "gpo_mlp_init",
+    "gpo_mlp_forward", "gpo_mlp_gradients", "gpo_mlp_train", "gpo_mlp_load",
 )
 
 
@@ -45,6 +46,8 @@ class Options(ctypes.Structure):
         ("node_budget", ctypes.c_uint64),
         ("split_min_empties", ctypes.c_int),
         ("wait_limit_ms", ctypes.c_int),
+        ("table_bits", ctypes.c_int),
+        ("table_min_empties", ctypes.c_int),
     ]
 
 
@@ -95,6 +98,13 @@ def lib():
         L.gpo_strerror.argtypes = [i]
         L.gpo_strerror.restype = ctypes.c_char_p
         L.gpo_device_info.argtypes = [ctypes.c_char_p, i, ctypes.POINTER(ctypes.c_int)]
+        f32 = ctypes.c_float
+        L.gpo_mlp_param_count.argtypes = []
+        L.gpo_mlp_init.argtypes = [u64, vp]
+        L.gpo_mlp_forward.argtypes = [vp, vp, vp, i, vp]
+        L.gpo_mlp_gradients.argtypes = [vp, vp, vp, vp, i, vp, ctypes.POINTER(f32)]
+        L.gpo_mlp_train.argtypes = [vp, vp, vp, i, i, i, f32, u64, vp, vp]
+        L.gpo_mlp_load.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -172,3 +182,59 @@ def device_info():
 
 def shutdown():
     lib().solve_shutdown()
+
+
+# ---- learned move orderer (mlp.cu) ----
+def mlp_init(seed):
+    w = np.zeros(lib().gpo_mlp_param_count(), np.float32)
+    rc = lib().gpo_mlp_init(seed, w.ctypes.data)
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_mlp_init")
+    return w
+
+
+def mlp_forward(w, player, opp):
+    p, o = _u64(player), _u64(opp)
+    z = np.zeros((len(p), 64), np.float32)
+    w = np.ascontiguousarray(w, np.float32)
+    rc = lib().gpo_mlp_forward(w.ctypes.data, p.ctypes.data, o.ctypes.data, len(p), z.ctypes.data)
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_mlp_forward")
+    return z
+
+
+def mlp_gradients(w, player, opp, best):
+    p, o = _u64(player), _u64(opp)
+    b = np.ascontiguousarray(best, np.int8)
+    w = np.ascontiguousarray(w, np.float32)
+    g = np.zeros_like(w)
+    loss = ctypes.c_float(0.0)
+    rc = lib().gpo_mlp_gradients(w.ctypes.data, p.ctypes.data, o.ctypes.data, b.ctypes.data, len(p),
+                                 g.ctypes.data, ctypes.byref(loss))
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_mlp_gradients")
+    return g, loss.value
+
+
+def mlp_train(player, opp, best, w, epochs=3, batch=4096, lr=1e-3, seed=0):
+    """Trains in place on a copy of w; returns (weights, [(loss, accuracy)] per epoch)."""
+    p, o = _u64(player), _u64(opp)
+    b = np.ascontiguousarray(best, np.int8)
+    w = np.array(w, np.float32)
+    hist = np.zeros(2 * epochs, np.float32)
+    rc = lib().gpo_mlp_train(p.ctypes.data, o.ctypes.data, b.ctypes.data, len(p), epochs, batch,
+                             lr, seed, w.ctypes.data, hist.ctypes.data)
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_mlp_train")
+    return w, [(float(hist[2 * e]), float(hist[2 * e + 1])) for e in range(epochs)]
+
+
+def mlp_load(w):
+    """Loads weights for the solver's learned root ordering (None unloads)."""
+    if w is None:
+        rc = lib().gpo_mlp_load(None)
+    else:
+        w = np.ascontiguousarray(w, np.float32)
+        rc = lib().gpo_mlp_load(w.ctypes.data)
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_mlp_load")

@@ -37,6 +37,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "search.cuh"
+#include "table.cuh"
 
 namespace gpo {
 
@@ -46,6 +47,7 @@ enum : int { OP_NONE = 0, OP_INIT, OP_MOVE, OP_PASS, OP_KEY, OP_REMASK, OP_DONAT
 enum : int { PH_INIT = 0, PH_MASK, PH_KEY, PH_LIST };
 
 constexpr int kFrameBytes = 20;
+constexpr int kRayBytes = 256 * 8;
 
 __device__ __forceinline__ unsigned pack_meta(int sq, int alpha, int beta, int best, int passed,
                                               int list) {
@@ -94,37 +96,7 @@ struct Frames {
 
 }  // namespace
 
-// Returns a finished task's value to its parent slot, walking up while this
-// lane is the last one holding the parent open; writes the input position's
-// score and best move at the top.  Every slot's accumulator holds the max
-// of its children's fail-soft candidates packed with the move that made
-// them; each candidate is either exact or a bound not above the true value
-// (its window's lower edge was a value already proven), so the max is the
-// node's fail-soft value and its move an optimal move.
-__device__ __forceinline__ void finish_slot(const BatchedArgs& a, unsigned slot) {
-  for (int guard = 0; guard < 2 * kMaxEmpties + 2; ++guard) {
-    __threadfence();
-    const unsigned packed = atomicAdd(&a.acc[slot], 0u);
-    const int v = static_cast<int>(packed >> 8) - 128;
-    if (slot < static_cast<unsigned>(a.n)) {
-      a.score[slot] = static_cast<signed char>(v);
-      if (a.best) a.best[slot] = static_cast<signed char>(packed & 255u);
-      __threadfence();
-      atomicAdd(&a.stats->done, 1u);
-      return;
-    }
-    const unsigned i = slot - static_cast<unsigned>(a.n);
-    const unsigned par = __ldcg(&a.parent[i]);
-    const unsigned msq = __ldcg(&a.psq[i]);
-    atomicMax(&a.acc[par], (static_cast<unsigned>(128 - v) << 8) | msq);
-    __threadfence();
-    if (atomicSub(&a.pending[par], 1u) != 1u) return;
-    slot = par;
-  }
-  atomicOr(&a.stats->status, kErrInternal);
-}
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+__device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
   return *reinterpret_cast<const volatile unsigned*>(p);
 }
 
@@ -134,8 +106,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+__device__ __forceinline__ unsigned pack_result(int v, int move) {
+  return (static_cast<unsigned>(v + 128) << 8) | static_cast<unsigned>(move & 255);
+}
+
 __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
-  extern __shared__ u64 smem_u64[];
+  extern __shared__ __align__(16) u64 smem_raw[];
+  u64* const rays = smem_raw;           // 64 x 4 up-ray table (bitboard.cuh)
+  u64* const smem_u64 = smem_raw + 256;  // frame slots
+  gpo_build_rays(rays);
+  __syncthreads();
   Frames fr;
   fr.B = blockDim.x;
   fr.t = threadIdx.x;
@@ -150,22 +130,43 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
   fr.gM = reinterpret_cast<u64*>(args.gframes);
   fr.gF = fr.gM + gslots * fr.G;
   fr.gX = reinterpret_cast<unsigned*>(fr.gF + gslots * fr.G);
+  const size_t G = fr.G, gid = fr.gid;
 
   const unsigned lane = threadIdx.x & 31;
   const unsigned lane_lt = (1u << lane) - 1u;
   const unsigned n = static_cast<unsigned>(args.n);
-  unsigned long long total_nodes = 0, donations = 0;
+  constexpr unsigned kNoMbox = 0xFFFFFFFFu;
+  unsigned long long total_nodes = 0, donations = 0, cancels = 0;
+  unsigned long long tt_probes = 0, tt_hits = 0, tt_updates = 0;
+  bool tt_cut = false;  // the current node was closed by a table bound when created
 
-  bool busy = false, waiting = false, exhausted = false, started = false;
-  unsigned slot = 0, top = 0, qidx = 0, chk = 0, dq = 0;
-  unsigned long long wait_start = 0;
+  // abort: close every open node of this lane's root at once (node budget
+  // exceeded, or the subtree was cancelled by its donor); an aborted
+  // subtree reports nothing but its completion.
+  bool busy = false, waiting = false, exhausted = false, started = false, abort = false;
+  unsigned pos = 0, task_mbox = kNoMbox, qidx = 0, chk = 0, dmask = 0;
+  int task_sq = 0;
+  // One deadline for the whole launch bounds every wait: a lane holding a
+  // ticket never gives it up early (a donor may still fill it), and when
+  // the deadline passes every lane unwinds and the call reports an error.
+  const unsigned long long deadline = global_ns() + args.wait_limit_ns;
+  bool late = false;
   u64 P = 0, O = 0, moves = 0, lst = 0, P0 = 0, O0 = 0;
   int alpha = 0, beta = 0, best = 0, passed = 0, E = 0, root_e = 0, phase = PH_INIT;
   int rootbest = kMoveNoneDev;
   unsigned long long nodes = 0;
 
   for (;;) {
-    // ---- lanes without work: input queue first (one atomic per warp) ----
+    // ---- lanes without work: a queued subtree first (hard positions split
+    //      early must not wait behind the input queue) ----
+    if (!busy && !waiting && !exhausted && args.donate_min > 0) {
+      const unsigned h = ld_volatile(&args.stats->dq_head);
+      if (h < ld_volatile(&args.stats->dq_tail) && atomicCAS(&args.stats->dq_head, h, h + 1u) == h) {
+        qidx = h;
+        waiting = true;
+      }
+    }
+    // ---- then the input queue (one atomic per warp) ----
     const unsigned need = __ballot_sync(0xffffffffu, !busy && !waiting && !exhausted);
     if (need) {
       const int leader = __ffs(need) - 1;
@@ -186,51 +187,50 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
             __threadfence();
             atomicAdd(&args.stats->done, 1u);
           } else {
-            busy = true;
-            started = true;
-            slot = p;
-            top = p;
+            busy = started = true;
+            pos = p;
+            task_mbox = kNoMbox;
             alpha = -64;
             beta = 64;
-            atomicExch(&args.acc[slot], 0u);
-            atomicExch(&args.pending[slot], 1u);
           }
         } else if (args.donate_min > 0) {
-          // nothing left to start: reserve the next donated task
-          qidx = atomicAdd(&args.stats->dq_head, 1u);
+          qidx = atomicAdd(&args.stats->dq_head, 1u);  // wait for a donated subtree
           waiting = true;
-          wait_start = global_ns();
         } else {
           exhausted = true;
         }
       }
     }
     if (waiting) {
-      if (qidx < args.task_cap && ld_acquire(&args.ready[qidx])) {
-        // Records and their side arrays were written by other SMs: read
-        // them from L2 (ld.global.cg), never from a possibly stale L1 line.
+      const unsigned qslot = qidx % args.task_cap;
+      if (ld_volatile(&args.ready[qslot]) == qidx + 1u) {
+        // The record was written by another SM: read it from L2 (.cg),
+        // never from a possibly stale L1 line.
         __threadfence();
-        const DonatedTask* q = args.queue + qidx;
-        waiting = false;
-        busy = true;
-        started = true;
+        const DonatedTask* q = args.queue + qslot;
         P = __ldcg(&q->player);
         O = __ldcg(&q->opp);
+        const unsigned w = __ldcg(&q->window);
+        task_mbox = __ldcg(&q->mbox);
+        pos = __ldcg(&q->top);
+        __threadfence();
+        atomicExch(&args.consumed[qslot], qidx + 1u);  // the record may be refilled
         E = 64 - popc(P | O);
-        alpha = __ldcg(&q->alpha);
-        beta = __ldcg(&q->beta);
-        slot = __ldcg(&q->slot);
-        top = __ldcg(&args.top[slot - n]);
-      } else if (ld_acquire(&args.stats->done) >= n) {
+        alpha = static_cast<signed char>(w & 0xff);
+        beta = static_cast<signed char>((w >> 8) & 0xff);
+        task_sq = static_cast<int>((w >> 16) & 0xff);
+        waiting = false;
+        busy = started = true;
+      } else if (ld_volatile(&args.stats->done) >= n) {
         waiting = false;
         exhausted = true;
-      } else if (global_ns() - wait_start > args.wait_limit_ns) {
+      } else if (global_ns() > deadline) {
         atomicOr(&args.stats->status, kErrWait);
         waiting = false;
         exhausted = true;
       }
     }
-    if (started) {  // a task was just taken: its root is this lane's level 0
+    if (started) {  // a position or subtree was just taken: it is this lane's root
       started = false;
       phase = PH_INIT;
       root_e = E;
@@ -240,37 +240,86 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
       passed = 0;
       nodes = 1;
       rootbest = kMoveNoneDev;
+      dmask = 0;
+      abort = false;
     }
-    const unsigned active = __ballot_sync(0xffffffffu, !exhausted);
-    if (active == 0) break;
-    if (__ballot_sync(0xffffffffu, busy) == 0) {
-      __nanosleep(256);  // a warp of waiting lanes leaves issue slots to busy warps
-      continue;
-    }
+    if (__ballot_sync(0xffffffffu, !exhausted) == 0) break;
 
     // ---- choose this lane's op; return finished nodes to their parents ----
     int op = OP_NONE, sq = 0;
-    int dalpha = 0, dbeta = 0;
+    u64 DX = 0, DY = 0;
+    unsigned dq = 0, dwin = 0, dmbox = 0;
     if (busy) {
       if (phase == PH_INIT) {
         op = OP_INIT;
       } else {
+        bool stall = false;
         for (;;) {
           bool more;
           if (phase == PH_KEY) more = true;
           else if (phase == PH_LIST) more = list_peek(moves) != 0xFFF || (moves & kListOverflow);
           else more = moves != 0;
           const bool fresh = best == -65;  // nothing searched yet
-          const bool finished = alpha >= beta || (!more && !fresh);
+          const bool finished = abort || alpha >= beta || (!more && !fresh);
           if (!finished) break;
-          const int r = passed ? -best : best;
-          if (E == root_e) {  // this lane's part of the task is done
-            if (args.nodes_out) atomicAdd(&args.nodes_out[top], nodes);
-            total_nodes += nodes;
-            atomicMax(&args.acc[slot], (static_cast<unsigned>(r + 128) << 8) |
-                                           static_cast<unsigned>(rootbest));
+          if ((dmask >> E) & 1u) {
+            // moves handed to other lanes must report before the node closes;
+            // after a cutoff (or an abort) their results no longer matter
+            const size_t mb = static_cast<size_t>(E) * G + gid;
+            if (ld_volatile(&args.mbox_pend[mb]) != 0u) {
+              bool cut = abort || alpha >= beta;
+              if (!cut) {
+                const unsigned a = ld_volatile(&args.mbox_acc[mb]);
+                cut = a && static_cast<int>(a >> 8) - 128 >= beta;
+              }
+              if (cut && !ld_volatile(&args.mbox_cancel[mb])) {
+                atomicExch(&args.mbox_cancel[mb], 1u);
+                ++cancels;
+              }
+              if (!late && global_ns() <= deadline) {
+                stall = true;
+                break;
+              }
+              late = true;
+              atomicOr(&args.stats->status, kErrWait);
+            }
             __threadfence();
-            if (atomicSub(&args.pending[slot], 1u) == 1u) finish_slot(args, slot);
+            const unsigned a = atomicAdd(&args.mbox_acc[mb], 0u);
+            if (a) {
+              const int v = static_cast<int>(a >> 8) - 128;
+              if (v > best) {
+                best = v;
+                if (E == root_e && !passed) rootbest = static_cast<int>(a & 255u);
+                if (v > alpha) alpha = v;
+              }
+            }
+            dmask &= ~(1u << E);
+          }
+          if (tt_cut) {
+            tt_cut = false;
+          } else if (args.tt_min && E >= args.tt_min && !passed && !abort) {
+            // best >= beta proves value >= best; anything lower proves
+            // value <= best (an exact value is also an upper bound)
+            const TTKey k = tt_key(P, O);
+            const bool ok = best >= beta ? tt_store(args.tt, args.tt_bits, k, best, 64)
+                                         : tt_store(args.tt, args.tt_bits, k, -64, best);
+            tt_updates += ok;
+          }
+          const int r = passed ? -best : best;
+          if (E == root_e) {  // the lane's root is done
+            if (args.nodes_out) atomicAdd(&args.nodes_out[pos], nodes);
+            total_nodes += nodes;
+            if (task_mbox == kNoMbox) {
+              args.score[pos] = static_cast<signed char>(abort ? (args.budget_mark ? -128 : 0) : r);
+              if (args.best) args.best[pos] = static_cast<signed char>(rootbest);
+              __threadfence();
+              atomicAdd(&args.stats->done, 1u);
+            } else {
+              if (!abort) atomicMax(&args.mbox_acc[task_mbox], pack_result(-r, task_sq));
+              __threadfence();
+              atomicSub(&args.mbox_pend[task_mbox], 1u);
+              atomicSub(&args.pos_tasks[pos], 1u);
+            }
             busy = false;
             break;
           }
@@ -300,54 +349,107 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
             if (v > alpha) alpha = v;
           }
         }
-        // ---- donation: hand an untried root move to a waiting lane ----
-        if (busy && E < root_e && root_e >= args.donate_min && args.donate_min > 0 &&
-            ((++chk) & 15u) == 0u) {
-          const int demand = static_cast<int>(ld_acquire(&args.stats->dq_head) -
-                                              ld_acquire(&args.stats->dq_tail));
-          if (demand > 0) {
-            u64 m0, f0;
-            unsigned meta0;
-            fr.load(root_e, m0, f0, meta0);
-            const int a0 = static_cast<signed char>((meta0 >> 6) & 0xff);
-            const int b0 = static_cast<signed char>((meta0 >> 14) & 0xff);
-            const int best0 = static_cast<signed char>((meta0 >> 22) & 0xff);
-            const unsigned accv = ld_acquire(&args.acc[slot]);
-            int lo0 = a0 > best0 ? a0 : best0;
-            if (accv) {
-              const int av = static_cast<int>(accv >> 8) - 128;
-              if (av > lo0) lo0 = av;
-            }
-            const bool root_passed = (meta0 >> 30) & 1u;
-            int dsq = -1;
-            u64 m1 = m0;
-            if (!root_passed && lo0 < b0) {
-              if (meta0 >> 31) {
-                const int e = list_peek(m0);
-                if (e != 0xFFF) {
-                  dsq = e & 63;
-                  m1 = m0 + (1ULL << 60);
+        // ---- a handed-out subtree whose donor was cut off stops early ----
+        ++chk;
+        if (busy && !abort && task_mbox != kNoMbox && (chk & 15u) == 0u &&
+            ld_volatile(&args.mbox_cancel[task_mbox]))
+          abort = true;
+        if (busy && !abort && (chk & 255u) == 0u && global_ns() > deadline) {
+          atomicOr(&args.stats->status, kErrWait);
+          late = abort = true;
+        }
+        // ---- donation: hand a move of an ancestor to a waiting lane ----
+        if (busy && !stall && !abort && E < root_e && args.donate_min > 0 &&
+            root_e >= args.donate_min && (chk & 15u) == 8u) {
+          const unsigned t = ld_volatile(&args.stats->dq_tail);
+          const unsigned h = ld_volatile(&args.stats->dq_head);
+          // Hand out a move when a lane waits for one (ticket t is held), or
+          // when this root has run long (a hard position: split it while
+          // the rest of the batch still keeps the GPU busy) and few records
+          // are queued; record t % cap must have been read by the holder of
+          // ticket t - cap.
+          const bool asked = t < h;
+          const bool pushed = !asked && nodes > args.long_nodes && t - h < 1024u;
+          if ((asked || pushed) && ld_volatile(&args.pos_tasks[pos]) < args.max_tasks &&
+              (t < args.task_cap ||
+               ld_volatile(&args.consumed[t % args.task_cap]) == t - args.task_cap + 1u)) {
+            // Walk the path from the root (replaying the stored flips) to the
+            // shallowest node whose first move has returned and that has an
+            // untried move.
+            u64 X = P0, Y = O0;
+            int de = -1;
+            u64 dm = 0, df = 0;
+            unsigned dmeta = 0;
+            int dlo = 0, db = 0;
+            for (int e = root_e; e > E; --e) {
+              u64 m, f;
+              unsigned meta;
+              fr.load(e, m, f, meta);
+              const int pas = static_cast<int>((meta >> 30) & 1u);
+              if (pas) {
+                const u64 tmp = X;
+                X = Y;
+                Y = tmp;
+              }
+              const int b0 = static_cast<signed char>((meta >> 14) & 0xff);
+              const int best0 = static_cast<signed char>((meta >> 22) & 0xff);
+              if (e >= args.donate_min && !pas && best0 > -65) {
+                const int a0 = static_cast<signed char>((meta >> 6) & 0xff);
+                int lo0 = a0 > best0 ? a0 : best0;
+                if ((dmask >> e) & 1u) {
+                  const unsigned a = ld_volatile(&args.mbox_acc[static_cast<size_t>(e) * G + gid]);
+                  if (a && static_cast<int>(a >> 8) - 128 > lo0) lo0 = static_cast<int>(a >> 8) - 128;
                 }
-              } else if (m0) {
-                const u64 b = pick_parity(m0, ~(P0 | O0));
-                dsq = ctz64(b);
-                m1 = m0 ^ b;
+                if (lo0 < b0) {
+                  if (meta >> 31) {
+                    const int en = list_peek(m);
+                    if (en != 0xFFF) {
+                      sq = en & 63;
+                      dm = m + (1ULL << 60);
+                      de = e;
+                    }
+                  } else if (m) {
+                    const u64 b = pick_parity(m, ~(X | Y));
+                    sq = ctz64(b);
+                    dm = m ^ b;
+                    de = e;
+                  }
+                  if (de >= 0) {
+                    df = f;
+                    dmeta = meta;
+                    dlo = lo0;
+                    db = b0;
+                    break;
+                  }
+                }
               }
+              const u64 bit = 1ULL << (meta & 63u);
+              const u64 cx = Y ^ f, cy = X ^ f ^ bit;
+              X = cx;
+              Y = cy;
             }
-            if (dsq >= 0) {
-              const unsigned qi = atomicAdd(&args.stats->dq_tail, 1u);
-              if (qi < args.task_cap) {
-                fr.store(root_e, m1, f0, meta0);
-                op = OP_DONATE;
-                sq = dsq;
-                dalpha = -b0;
-                dbeta = -lo0;
-                dq = qi;
+            if (de >= 0 && atomicCAS(&args.stats->dq_tail, t, t + 1u) == t) {
+              fr.store(de, dm, df, dmeta);
+              const size_t mb = static_cast<size_t>(de) * G + gid;
+              if (!((dmask >> de) & 1u)) {
+                atomicExch(&args.mbox_acc[mb], 0u);
+                atomicExch(&args.mbox_pend[mb], 0u);
+                atomicExch(&args.mbox_cancel[mb], 0u);
+                dmask |= 1u << de;
               }
+              atomicAdd(&args.mbox_pend[mb], 1u);
+              atomicAdd(&args.pos_tasks[pos], 1u);
+              op = OP_DONATE;
+              DX = X;
+              DY = Y;
+              dq = t;
+              dmbox = static_cast<unsigned>(mb);
+              dwin = static_cast<unsigned>((-db) & 0xff) | (static_cast<unsigned>((-dlo) & 0xff) << 8) |
+                     (static_cast<unsigned>(sq) << 16);
             }
           }
         }
-        if (busy && op == OP_NONE) {
+        if (busy && !stall && op == OP_NONE) {
           if (phase == PH_KEY) {
             const u64 b = moves & (0ULL - moves);
             moves ^= b;
@@ -373,14 +475,18 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
         }
       }
     }
+    if (!__any_sync(0xffffffffu, op != OP_NONE)) {
+      __nanosleep(200);  // idle or waiting warp: leave issue slots to busy warps
+      continue;
+    }
 
     // ---- the uniform heavy step: one flip, one mobility ----
     const bool play = op == OP_MOVE || op == OP_KEY || op == OP_DONATE;
     const bool same = op == OP_INIT || op == OP_REMASK;
-    const u64 X = op == OP_DONATE ? P0 : P;
-    const u64 Y = op == OP_DONATE ? O0 : O;
+    const u64 X = op == OP_DONATE ? DX : P;
+    const u64 Y = op == OP_DONATE ? DY : O;
     const u64 bit = play ? (1ULL << sq) : 0ULL;
-    const u64 f = play ? gpo_flip(X, Y, sq) : 0ULL;
+    const u64 f = play ? gpo_flip(X, Y, sq, rays) : 0ULL;
     const u64 cP = same ? X : (Y ^ f);
     const u64 cO = same ? Y : (X ^ f ^ bit);
     const u64 cm = gpo_mobility(cP, cO);
@@ -391,24 +497,16 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
     // and `lst` the list being built; the list replaces `moves` when done.
     bool start_keys = false;
     if (op == OP_DONATE) {
-      const unsigned qi = dq;
-      const unsigned ns = n + qi;
-      atomicAdd(&args.pending[slot], 1u);
-      atomicExch(&args.acc[ns], 0u);
-      atomicExch(&args.pending[ns], 1u);
-      args.parent[qi] = slot;
-      args.psq[qi] = static_cast<unsigned char>(sq);
-      args.top[qi] = top;
-      DonatedTask tk;
-      tk.player = cP;
-      tk.opp = cO;
-      tk.alpha = dalpha;
-      tk.beta = dbeta;
-      tk.slot = ns;
-      tk.pad = 0;
-      args.queue[qi] = tk;
+      const unsigned qslot = dq % args.task_cap;
+      DonatedTask* q = args.queue + qslot;
+      q->player = cP;
+      q->opp = cO;
+      q->window = dwin;
+      q->mbox = dmbox;
+      q->top = pos;
+      q->pad = 0;
       __threadfence();
-      atomicExch(&args.ready[qi], 1u);
+      atomicExch(&args.ready[qslot], dq + 1u);
       ++donations;
     } else if (op == OP_KEY) {
       int k = popc(cm) * 2 + ((bit & kCorners) ? 0 : 1);
@@ -422,6 +520,11 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
       moves = cm;
       phase = PH_MASK;
       start_keys = cm && E >= args.ff;
+      if (cm && args.root_lists && task_mbox == kNoMbox && E >= args.learned_min) {
+        moves = args.root_lists[pos];  // the learned orderer's five best moves
+        phase = PH_LIST;
+        start_keys = false;
+      }
     } else if (op == OP_REMASK) {
       moves = cm & ~list_squares(moves);
       phase = PH_MASK;
@@ -465,15 +568,30 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
         moves = cm;
         phase = PH_MASK;
         start_keys = cm && E >= args.ff;
-        if (args.node_budget && nodes > args.node_budget) {
-          // watchdog: give up on this task; its chain still completes so
-          // every lane finishes, and the call reports the error
-          atomicOr(&args.stats->status, kErrBudget);
-          E = root_e;
-          best = 0;
-          alpha = beta;  // finishes at once on the next iteration
-          passed = 0;
-          rootbest = kMoveNoneDev;
+        if (args.tt_min && E >= args.tt_min && !abort) {
+          int lb, ub;
+          ++tt_probes;
+          if (tt_probe(args.tt, args.tt_bits, tt_key(P, O), lb, ub)) {
+            ++tt_hits;
+            // a bound outside the window closes the node at once; one
+            // inside narrows it (sound for fail-soft search)
+            if (lb >= beta || ub <= alpha || lb >= ub) {
+              best = lb >= beta ? lb : (ub <= alpha ? ub : lb);
+              alpha = beta;
+              tt_cut = true;
+              start_keys = false;
+            } else {
+              if (lb > alpha) alpha = lb;
+              if (ub < beta) beta = ub;
+            }
+          }
+        }
+        if (args.node_budget && nodes > args.node_budget && !abort) {
+          // watchdog: every open node of this lane closes at once (still
+          // collecting any handed-out moves); the call reports the error,
+          // or, in a first pass, the position is marked for the second
+          if (!args.budget_mark) atomicOr(&args.stats->status, kErrBudget);
+          abort = true;
         }
       }
     }
@@ -484,11 +602,15 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
   }
   warp_add(&args.stats->nodes, total_nodes);
   warp_add(&args.stats->donations, donations);
+  warp_add(&args.stats->cancels, cancels);
+  warp_add(&args.stats->tt_probes, tt_probes);
+  warp_add(&args.stats->tt_hits, tt_hits);
+  warp_add(&args.stats->tt_updates, tt_updates);
 }
 
 cudaError_t batched_grid(int threads, int smem_top, int sms, int* grid, size_t* smem) {
   const int sslots = smem_top >= 2 ? smem_top - 1 : 0;
-  *smem = static_cast<size_t>(threads) * sslots * kFrameBytes;
+  *smem = kRayBytes + static_cast<size_t>(threads) * sslots * kFrameBytes;
   cudaError_t e = cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(*smem));
   if (e != cudaSuccess) return e;
@@ -512,7 +634,7 @@ cudaError_t batched_plan(int threads, int depth, int* smem_top) {
     e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  const int per_block = smem_sm / per_sm - 1024;  // 1 KB per block is reserved
+  const int per_block = smem_sm / per_sm - 1024 - kRayBytes;  // 1 KB per block is reserved
   const int slots = per_block > 0 ? per_block / (threads * kFrameBytes) : 0;
   int top = slots + 1;
   if (top > depth) top = depth;

@@ -9,12 +9,9 @@
 //   gpo_final      disc difference at game end, empties to the winner
 //                                             (board.cuh:7-18)
 //
-// The ray geometry constants are the squares k*s (k = 1..7) reached from
-// square 0 by steps s = 1, 7, 8, 9 ("up", toward higher bits) and the mirror
-// set 63 - k*s ("down", toward lower bits).  Horizontal and diagonal runs can
-// only flank interior discs, so the opponent set is clipped to columns B..G
-// for those lines; every scan then stops at an edge column at the latest and
-// the masks need no per-square clipping.
+// Mobility: horizontal and diagonal runs can only flank interior discs, so
+// the opponent set is clipped to columns B..G for those lines and no shift
+// can carry a run across the board edge.
 #pragma once
 #include <cstdint>
 
@@ -50,34 +47,52 @@ __device__ __forceinline__ u64 gpo_mobility(u64 P, u64 O) {
 }
 
 // ---- flip ----
-// Up ray (higher bits): the first square along the ray that is not an
-// opponent disc is found with a carry: (Om | ~ray) + 1 clears every bit
-// below it and sets it.  Down ray (lower bits): the first such square is
-// the highest set bit of ~Om & ray.
+// Rays toward higher bits ("up": +8, +1, +7, +9) use a carry: the first
+// square along the ray that is not an opponent disc is the lowest set bit of
+// (Om | ~ray) + 1 within the ray.  Rays toward lower bits are the up rays of
+// the mirrored square 63 - sq on the bit-reversed board (reversing the bit
+// order rotates the board by 180 degrees, which maps south/west/south-east/
+// south-west onto north/east/north-west/north-east), so all eight directions
+// use the carry form.
+//
+// `rays` is the per-square up-ray table built by gpo_build_rays (in shared
+// memory): rays[4*sq + k] for k = 0..3 = the squares beyond sq toward +8,
+// +1, +7, +9.  Loading it runs on the load/store pipe, which the search
+// leaves idle, instead of four variable 64-bit shifts on the integer pipe.
 __device__ __forceinline__ u64 flip_up(u64 P, u64 Om, u64 ray) {
   const u64 outflank = ((Om | ~ray) + 1) & ray & P;
   return outflank ? ((outflank - 1) & ray) : 0ULL;
 }
 
-__device__ __forceinline__ u64 flip_down(u64 P, u64 Om, u64 ray) {
-  const u64 stop = ~Om & ray;
-  const u64 top = stop ? (0x8000000000000000ULL >> __clzll(stop)) : 0ULL;
-  const u64 outflank = top & P;
-  return (0ULL - outflank - outflank) & ray;  // ray squares above outflank
+// The table's rays stop at the board edge, so no column mask is needed.
+__device__ __forceinline__ u64 flip_up4(u64 P, u64 O, const u64* r) {
+  const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(r);
+  const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(r + 2);
+  return flip_up(P, O, a.x) | flip_up(P, O, a.y) | flip_up(P, O, b.x) | flip_up(P, O, b.y);
 }
 
-__device__ __forceinline__ u64 gpo_flip(u64 P, u64 O, int sq) {
-  const u64 Oi = O & 0x7e7e7e7e7e7e7e7eULL;
-  const int dn = 63 - sq;
-  u64 f = flip_up(P, O, 0x0101010101010100ULL << sq);
-  f |= flip_up(P, Oi, 0x00000000000000feULL << sq);
-  f |= flip_up(P, Oi, 0x0002040810204080ULL << sq);
-  f |= flip_up(P, Oi, 0x8040201008040200ULL << sq);
-  f |= flip_down(P, O, 0x0080808080808080ULL >> dn);
-  f |= flip_down(P, Oi, 0x7f00000000000000ULL >> dn);
-  f |= flip_down(P, Oi, 0x0102040810204000ULL >> dn);
-  f |= flip_down(P, Oi, 0x0040201008040201ULL >> dn);
-  return f;
+__device__ __forceinline__ u64 gpo_flip(u64 P, u64 O, int sq, const u64* rays) {
+  const u64 up = flip_up4(P, O, rays + 4 * sq);
+  const u64 dn = flip_up4(__brevll(P), __brevll(O), rays + 4 * (63 - sq));
+  return up | __brevll(dn);
+}
+
+// Fills the 64 x 4 up-ray table (256 words) cooperatively; the caller
+// synchronises the block afterwards.
+__device__ __forceinline__ void gpo_build_rays(u64* rays) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    const int sq = i >> 2, k = i & 3;
+    const int dr = k == 1 ? 0 : 1;
+    const int dc = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? -1 : 1));
+    u64 m = 0;
+    int r = sq / 8 + dr, c = sq % 8 + dc;
+    while (r >= 0 && r < 8 && c >= 0 && c < 8) {
+      m |= 1ULL << (r * 8 + c);
+      r += dr;
+      c += dc;
+    }
+    rays[i] = m;
+  }
 }
 
 // Exact final score: disc difference with the empties awarded to the
@@ -89,10 +104,10 @@ __device__ __forceinline__ int gpo_final(u64 P, u64 O) {
 
 // Score after the last empty square `sq` is filled (or passed on).  With one
 // empty the disc difference after a move follows from the flip count alone.
-__device__ __forceinline__ int gpo_solve1(u64 P, u64 O, int sq) {
-  int n = popc(gpo_flip(P, O, sq));
+__device__ __forceinline__ int gpo_solve1(u64 P, u64 O, int sq, const u64* rays) {
+  int n = popc(gpo_flip(P, O, sq, rays));
   if (n) return 2 * (popc(P) + n + 1) - 64;
-  n = popc(gpo_flip(O, P, sq));
+  n = popc(gpo_flip(O, P, sq, rays));
   if (n) return 64 - 2 * (popc(O) + n + 1);
   return gpo_final(P, O);
 }

@@ -35,19 +35,30 @@ struct Context {
   DeviceStats* dStats = nullptr;
   unsigned char* dFrames = nullptr;  // batched kernel's global frame slots
   size_t frames_cap = 0;
-  // work donation: accumulators for n + task_cap slots, queue of task_cap
+  // work donation: mailboxes (33 per lane), queue records
   unsigned task_cap = 0;
-  size_t slot_cap = 0;
-  unsigned* dAcc = nullptr;
-  unsigned* dPending = nullptr;
-  unsigned* dParent = nullptr;
-  unsigned char* dPsq = nullptr;
-  unsigned* dTop = nullptr;
+  size_t mbox_cap = 0;
+  unsigned* dMboxAcc = nullptr;
+  unsigned* dMboxPend = nullptr;
+  unsigned* dMboxCancel = nullptr;
   DonatedTask* dQueue = nullptr;
   unsigned* dReady = nullptr;
+  unsigned* dConsumed = nullptr;
+  unsigned* dPosTasks = nullptr;  // per input position (capacity cap)
+  unsigned long long* dTable = nullptr;  // transposition table
+  int table_bits = 0;
+  u64* dLists = nullptr;  // learned root orders (capacity cap)
+  // second pass (hard positions)
+  size_t second_cap = 0;
+  unsigned* d2Idx = nullptr;
+  u64* d2P = nullptr;
+  u64* d2O = nullptr;
+  signed char* d2Score = nullptr;
+  signed char* d2Best = nullptr;
+  unsigned long long* d2Nodes = nullptr;
 };
 
-constexpr unsigned kTaskCap = 1u << 22;  // donated subtrees per call
+constexpr unsigned kTaskCap = 1u << 20;  // queue records (a ring, reused within a call)
 
 std::mutex g_mutex;
 Context* g_ctx = nullptr;
@@ -64,38 +75,62 @@ int cuda_fail(cudaError_t e, const char* what) {
   } while (0)
 
 void free_donation(Context* c) {
-  cudaFree(c->dAcc);
-  cudaFree(c->dPending);
-  cudaFree(c->dParent);
-  cudaFree(c->dPsq);
-  cudaFree(c->dTop);
+  cudaFree(c->dMboxAcc);
+  cudaFree(c->dMboxPend);
+  cudaFree(c->dMboxCancel);
   cudaFree(c->dQueue);
   cudaFree(c->dReady);
-  c->dAcc = c->dPending = c->dParent = c->dTop = c->dReady = nullptr;
-  c->dPsq = nullptr;
+  cudaFree(c->dConsumed);
+  c->dConsumed = nullptr;
+  c->dMboxAcc = c->dMboxPend = c->dMboxCancel = c->dReady = nullptr;
   c->dQueue = nullptr;
   c->task_cap = 0;
-  c->slot_cap = 0;
+  c->mbox_cap = 0;
 }
 
-int ensure_donation(Context* c, size_t n) {
-  const size_t slots = n + kTaskCap;
-  if (c->task_cap == kTaskCap && c->slot_cap >= slots) return GPO_OK;
+// Mailboxes for `lanes` grid threads and the record queue.
+int ensure_donation(Context* c, size_t lanes) {
+  const size_t mboxes = static_cast<size_t>(kMaxEmpties + 1) * lanes;
+  if (c->task_cap == kTaskCap && c->mbox_cap >= mboxes) return GPO_OK;
   free_donation(c);
-  GPO_CK(cudaMalloc(&c->dAcc, slots * sizeof(unsigned)));
-  GPO_CK(cudaMalloc(&c->dPending, slots * sizeof(unsigned)));
-  GPO_CK(cudaMalloc(&c->dParent, kTaskCap * sizeof(unsigned)));
-  GPO_CK(cudaMalloc(&c->dPsq, kTaskCap));
-  GPO_CK(cudaMalloc(&c->dTop, kTaskCap * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dMboxAcc, mboxes * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dMboxPend, mboxes * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dMboxCancel, mboxes * sizeof(unsigned)));
   GPO_CK(cudaMalloc(&c->dQueue, kTaskCap * sizeof(DonatedTask)));
   GPO_CK(cudaMalloc(&c->dReady, kTaskCap * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dConsumed, kTaskCap * sizeof(unsigned)));
   c->task_cap = kTaskCap;
-  c->slot_cap = slots;
+  c->mbox_cap = mboxes;
+  return GPO_OK;
+}
+
+int ensure_table(Context* c, int bits) {
+  if (c->dTable && c->table_bits == bits) return GPO_OK;
+  cudaFree(c->dTable);
+  c->dTable = nullptr;
+  c->table_bits = 0;
+  GPO_CK(cudaMalloc(&c->dTable, (static_cast<size_t>(16)) << bits));
+  c->table_bits = bits;
   return GPO_OK;
 }
 
 void free_buffers(Context* c) {
   free_donation(c);
+  cudaFree(c->d2Idx);
+  cudaFree(c->d2P);
+  cudaFree(c->d2O);
+  cudaFree(c->d2Score);
+  cudaFree(c->d2Best);
+  cudaFree(c->d2Nodes);
+  c->d2Idx = nullptr;
+  c->d2P = c->d2O = nullptr;
+  c->d2Score = c->d2Best = nullptr;
+  c->d2Nodes = nullptr;
+  c->second_cap = 0;
+  cudaFree(c->dPosTasks);
+  c->dPosTasks = nullptr;
+  cudaFree(c->dLists);
+  c->dLists = nullptr;
   cudaFree(c->dFrames);
   c->dFrames = nullptr;
   c->frames_cap = 0;
@@ -149,6 +184,8 @@ int ensure_capacity(Context* c, size_t n) {
   GPO_CK(cudaMalloc(&c->dBest, cap));
   GPO_CK(cudaMalloc(&c->dNodes, cap * sizeof(unsigned long long)));
   GPO_CK(cudaMalloc(&c->dPerm, cap * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dPosTasks, cap * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->dLists, cap * sizeof(u64)));
   c->cap = cap;
   return GPO_OK;
 }
@@ -163,6 +200,7 @@ int status_to_error(unsigned st) {
 
 int check_options(const gpo_options* opt) {
   if (!opt) return GPO_OK;
+  if (opt->table_bits != 0 && (opt->table_bits < 16 || opt->table_bits > 31)) return GPO_ERR_ARG;
   if (opt->method != GPO_METHOD_BATCHED && opt->method != GPO_METHOD_PLAIN) return GPO_ERR_ARG;
   if (opt->threads_per_block != 0 &&
       (opt->threads_per_block < 32 || opt->threads_per_block > 1024 || opt->threads_per_block % 32))
@@ -170,83 +208,206 @@ int check_options(const gpo_options* opt) {
   return GPO_OK;
 }
 
-// Runs the solve pipeline on device arrays already in place.
+struct PassResult {
+  DeviceStats hs = {};
+  float ms = 0.f;  // search kernel time
+  unsigned long long learned = 0;
+};
+
+struct PassConfig {
+  unsigned long long budget;  // per-position node budget (0 = none)
+  bool mark;                  // over budget: score -128 instead of an error
+  bool split;                 // hand subtrees of hard positions to idle lanes
+  bool clear_table;           // clear the transposition table first
+};
+
+// One batched pass over device arrays already in place: bucketing, learned
+// root orders, the persistent search; waits for it and returns its status.
+int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+             signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
+             const PassConfig& pc, cudaStream_t s, PassResult* pr) {
+  GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
+  GPO_CK(cudaMemsetAsync(c->dHist, 0, 65 * sizeof(unsigned), s));
+  GPO_CK(launch_bucket(dP, dO, n, depth, c->dHist, c->dCursor, c->dPerm, c->dStats, c->sms, s));
+  // Learned root orders for the positions with >= learned_min empties
+  // (the front of the bucketed queue).
+  const int lmin = o.learned_min_empties > 0 ? o.learned_min_empties : 14;
+  const bool learned = (o.use_learned > 0 || (o.use_learned < 0 && mlp_loaded())) && depth >= lmin;
+  long learned_count = 0;
+  if (learned) {
+    if (!mlp_loaded()) return GPO_ERR_ARG;
+    unsigned hist[65];
+    GPO_CK(cudaMemcpyAsync(hist, c->dHist, sizeof(hist), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    for (int e = lmin; e <= 64; ++e) learned_count += hist[e];
+    if (learned_count > 0) {
+      const int rcl = mlp_order_roots(dP, dO, c->dPerm, learned_count, c->dLists, s);
+      if (rcl != GPO_OK) return rcl;
+      pr->learned = static_cast<unsigned long long>(learned_count);
+    }
+  }
+  BatchedArgs a = {};
+  a.player = dP;
+  a.opp = dO;
+  a.perm = c->dPerm;
+  a.n = n;
+  a.depth = depth;
+  a.ff = o.fastest_first_empties > 0 ? o.fastest_first_empties : 9;
+  a.score = dScore;
+  a.best = dBest;
+  a.nodes_out = dNodes;
+  a.stats = c->dStats;
+  a.node_budget = pc.budget;
+  a.budget_mark = pc.mark ? 1 : 0;
+  BatchedLaunch cfg;
+  cfg.threads = o.threads_per_block > 0 ? o.threads_per_block : 128;
+  GPO_CK(batched_plan(cfg.threads, depth, &a.smem_top));
+  cfg.grid = 0;
+  size_t smem = 0;
+  GPO_CK(batched_grid(cfg.threads, a.smem_top, c->sms, &cfg.grid, &smem));
+  const size_t need = static_cast<size_t>(depth > a.smem_top ? depth - a.smem_top : 0) *
+                      static_cast<size_t>(cfg.grid) * cfg.threads * 20;
+  if (need > c->frames_cap) {
+    cudaFree(c->dFrames);
+    c->dFrames = nullptr;
+    c->frames_cap = 0;
+    GPO_CK(cudaMalloc(&c->dFrames, need));
+    c->frames_cap = need;
+  }
+  a.gframes = c->dFrames;
+  a.root_lists = learned_count > 0 ? c->dLists : nullptr;
+  a.learned_min = lmin;
+  if (pc.split) {
+    const int rcd = ensure_donation(c, static_cast<size_t>(cfg.grid) * cfg.threads);
+    if (rcd != GPO_OK) return rcd;
+    a.donate_min = o.split_min_empties > 0 ? o.split_min_empties : 12;
+    a.long_nodes = 1ULL << 21;
+    a.pos_tasks = c->dPosTasks;
+    // At most 32 handed-out subtrees per position: more lanes than that on
+    // one position cost more in stale-window search than they save.
+    a.max_tasks = 32;
+    a.task_cap = c->task_cap;
+    a.mbox_acc = c->dMboxAcc;
+    a.mbox_pend = c->dMboxPend;
+    a.mbox_cancel = c->dMboxCancel;
+    a.queue = c->dQueue;
+    a.ready = c->dReady;
+    a.consumed = c->dConsumed;
+    GPO_CK(cudaMemsetAsync(c->dPosTasks, 0, static_cast<size_t>(n) * sizeof(unsigned), s));
+    GPO_CK(cudaMemsetAsync(c->dReady, 0, static_cast<size_t>(c->task_cap) * sizeof(unsigned), s));
+    GPO_CK(cudaMemsetAsync(c->dConsumed, 0, static_cast<size_t>(c->task_cap) * sizeof(unsigned), s));
+  }
+  const bool table = o.use_table > 0;
+  if (table) {
+    const int bits = o.table_bits > 0 ? o.table_bits : 24;
+    const int rct = ensure_table(c, bits);
+    if (rct != GPO_OK) return rct;
+    if (pc.clear_table) GPO_CK(cudaMemsetAsync(c->dTable, 0, static_cast<size_t>(16) << bits, s));
+    a.tt = c->dTable;
+    a.tt_bits = bits;
+    a.tt_min = o.table_min_empties > 0 ? o.table_min_empties : 11;
+  }
+  a.wait_limit_ns =
+      static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 600000) * 1000000ULL;
+  if (dNodes) GPO_CK(cudaMemsetAsync(dNodes, 0, static_cast<size_t>(n) * sizeof(u64), s));
+  GPO_CK(cudaEventRecord(c->ev0, s));
+  GPO_CK(launch_batched(a, cfg, c->sms, s));
+  GPO_CK(cudaEventRecord(c->ev1, s));
+  GPO_CK(cudaMemcpyAsync(&pr->hs, c->dStats, sizeof(pr->hs), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  cudaEventElapsedTime(&pr->ms, c->ev0, c->ev1);
+  return status_to_error(pr->hs.status);
+}
+
+int ensure_second(Context* c, size_t n) {
+  if (n <= c->second_cap) return GPO_OK;
+  cudaFree(c->d2Idx);
+  cudaFree(c->d2P);
+  cudaFree(c->d2O);
+  cudaFree(c->d2Score);
+  cudaFree(c->d2Best);
+  cudaFree(c->d2Nodes);
+  c->second_cap = 0;
+  GPO_CK(cudaMalloc(&c->d2Idx, n * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&c->d2P, n * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->d2O, n * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->d2Score, n));
+  GPO_CK(cudaMalloc(&c->d2Best, n));
+  GPO_CK(cudaMalloc(&c->d2Nodes, n * sizeof(u64)));
+  c->second_cap = n;
+  return GPO_OK;
+}
+
+// Runs the solve pipeline on device arrays already in place.  Batched
+// method: a first pass gives every position a node budget; the few hard
+// positions that exceed it are solved again in a second pass in which idle
+// lanes split them (their first-pass search is discarded, the table keeps
+// what it learned).  With a caller node budget, or splitting off, one pass.
 int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
               signed char* dBest, unsigned long long* dNodes, const gpo_options* opt,
               gpo_stats* stats, cudaStream_t s) {
   gpo_options o;
   gpo_default_options(&o);
   if (opt) o = *opt;
-  // ev0/ev1 bracket the search kernel only (kernel_ms)
-  GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
   if (o.method == GPO_METHOD_PLAIN) {
+    GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
     GPO_CK(cudaEventRecord(c->ev0, s));
     GPO_CK(launch_plain(dP, dO, n, depth, dScore, dNodes, c->dStats, s));
-  } else {
-    GPO_CK(cudaMemsetAsync(c->dHist, 0, 65 * sizeof(unsigned), s));
-    GPO_CK(launch_bucket(dP, dO, n, depth, c->dHist, c->dCursor, c->dPerm, c->dStats, c->sms, s));
-    GPO_CK(cudaEventRecord(c->ev0, s));
-    BatchedArgs a;
-    a.player = dP;
-    a.opp = dO;
-    a.perm = c->dPerm;
-    a.n = n;
-    a.depth = depth;
-    a.ff = o.fastest_first_empties > 0 ? o.fastest_first_empties : 9;
-    a.score = dScore;
-    a.best = dBest;
-    a.nodes_out = dNodes;
-    a.stats = c->dStats;
-    a.node_budget = o.node_budget;
-    BatchedLaunch cfg;
-    cfg.threads = o.threads_per_block > 0 ? o.threads_per_block : 128;
-    GPO_CK(batched_plan(cfg.threads, depth, &a.smem_top));
-    cfg.grid = 0;
-    size_t smem = 0;
-    GPO_CK(batched_grid(cfg.threads, a.smem_top, c->sms, &cfg.grid, &smem));
-    const size_t need = static_cast<size_t>(depth > a.smem_top ? depth - a.smem_top : 0) *
-                        static_cast<size_t>(cfg.grid) * cfg.threads * 20;
-    if (need > c->frames_cap) {
-      cudaFree(c->dFrames);
-      c->dFrames = nullptr;
-      c->frames_cap = 0;
-      GPO_CK(cudaMalloc(&c->dFrames, need));
-      c->frames_cap = need;
+    GPO_CK(cudaEventRecord(c->ev1, s));
+    DeviceStats hs;
+    GPO_CK(cudaMemcpyAsync(&hs, c->dStats, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    if (stats) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+      stats->nodes = hs.nodes;
+      stats->kernel_ms = ms;
     }
-    a.gframes = c->dFrames;
-    const int rcd = ensure_donation(c, static_cast<size_t>(n));
-    if (rcd != GPO_OK) return rcd;
-    a.donate_min = o.split_min_empties < 0 ? 0 : (o.split_min_empties > 0 ? o.split_min_empties : 10);
-    a.task_cap = c->task_cap;
-    a.acc = c->dAcc;
-    a.pending = c->dPending;
-    a.parent = c->dParent;
-    a.psq = c->dPsq;
-    a.top = c->dTop;
-    a.queue = c->dQueue;
-    a.ready = c->dReady;
-    a.wait_limit_ns = static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 120000) *
-                      1000000ULL;
-    GPO_CK(cudaMemsetAsync(c->dReady, 0, static_cast<size_t>(c->task_cap) * sizeof(unsigned), s));
-    if (dNodes) GPO_CK(cudaMemsetAsync(dNodes, 0, static_cast<size_t>(n) * sizeof(u64), s));
-    GPO_CK(launch_batched(a, cfg, c->sms, s));
+    return status_to_error(hs.status);
   }
-  GPO_CK(cudaEventRecord(c->ev1, s));
-  DeviceStats hs;
-  GPO_CK(cudaMemcpyAsync(&hs, c->dStats, sizeof(hs), cudaMemcpyDeviceToHost, s));
-  GPO_CK(cudaStreamSynchronize(s));
+  const bool split = o.split_min_empties >= 0;
+  const bool two_pass = split && o.node_budget == 0;
+  PassConfig p1;
+  p1.budget = two_pass ? (1ULL << 22) : o.node_budget;
+  p1.mark = two_pass;
+  p1.split = split && !two_pass;
+  p1.clear_table = true;
+  PassResult r1;
+  int rc = run_pass(c, dP, dO, n, depth, dScore, dBest, dNodes, o, p1, s, &r1);
+  PassResult r2;
+  if (rc == GPO_OK && two_pass) {
+    unsigned count = 0;
+    GPO_CK(ensure_second(c, static_cast<size_t>(n)) == GPO_OK ? cudaSuccess : cudaErrorMemoryAllocation);
+    GPO_CK(launch_collect_marked(dScore, n, c->d2Idx, c->dCursor, s));
+    GPO_CK(cudaMemcpyAsync(&count, c->dCursor, sizeof(count), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    if (count > 0) {
+      const int m = static_cast<int>(count);
+      GPO_CK(launch_gather(dP, dO, c->d2Idx, m, c->d2P, c->d2O, s));
+      PassConfig p2;
+      p2.budget = 0;
+      p2.mark = false;
+      p2.split = true;
+      p2.clear_table = false;
+      rc = run_pass(c, c->d2P, c->d2O, m, depth, c->d2Score, dBest ? c->d2Best : nullptr,
+                    dNodes ? c->d2Nodes : nullptr, o, p2, s, &r2);
+      if (rc == GPO_OK || rc == GPO_ERR_TIMEOUT) {
+        GPO_CK(launch_scatter_scores(c->d2Score, c->d2Best, c->d2Nodes, c->d2Idx, m, dScore,
+                                     dBest, dNodes, s));
+        GPO_CK(cudaStreamSynchronize(s));
+      }
+    }
+  }
   if (stats) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    stats->nodes = hs.nodes;
-    stats->table_probes = hs.tt_probes;
-    stats->table_hits = hs.tt_hits;
-    stats->table_updates = hs.tt_updates;
-    stats->learned_calls = hs.learned_calls;
-    stats->splits = hs.donations;
-    stats->kernel_ms = ms;
+    stats->nodes = r1.hs.nodes + r2.hs.nodes;
+    stats->table_probes = r1.hs.tt_probes + r2.hs.tt_probes;
+    stats->table_hits = r1.hs.tt_hits + r2.hs.tt_hits;
+    stats->table_updates = r1.hs.tt_updates + r2.hs.tt_updates;
+    stats->learned_calls = r1.learned + r2.learned;
+    stats->splits = r1.hs.donations + r2.hs.donations;
+    stats->kernel_ms = r1.ms + r2.ms;
   }
-  return status_to_error(hs.status);
+  return rc;
 }
 
 int validate_call(const void* a, const void* b, const void* out, int n, int depth) {
@@ -370,6 +531,7 @@ void solve_shutdown(void) {
   Context* c = g_ctx;
   cudaStreamSynchronize(c->stream);
   free_buffers(c);
+  cudaFree(c->dTable);
   cudaFree(c->dHist);
   cudaFree(c->dCursor);
   cudaFree(c->dStats);
@@ -388,7 +550,7 @@ const char* gpo_strerror(int status) {
     case GPO_ERR_BOARD: return "a square is occupied by both sides";
     case GPO_ERR_CUDA: return "CUDA runtime error";
     case GPO_ERR_NOMEM: return "out of memory";
-    case GPO_ERR_TIMEOUT: return "node budget exceeded";
+    case GPO_ERR_TIMEOUT: return "node budget or wait limit exceeded";
     case GPO_ERR_INTERNAL: return "internal consistency check failed";
     case GPO_ERR_IO: return "file I/O error";
     default: return "unknown status";

@@ -39,9 +39,9 @@ struct DeviceStats {
   unsigned int next;         // work-queue cursor of the persistent kernel
   unsigned int done;         // input positions finished
   unsigned int dq_head;      // donation queue: records reserved by idle lanes
-  unsigned int dq_tail;      // donation queue: records written by donors
-  unsigned int task_count;   // donated task slots handed out
+  unsigned int dq_tail;      // donation queue: records claimed by donors
   unsigned long long donations;
+  unsigned long long cancels;    // handed-out subtrees abandoned after a cutoff
 };
 
 __device__ __forceinline__ int ctz64(u64 x) { return __ffsll(static_cast<long long>(x)) - 1; }

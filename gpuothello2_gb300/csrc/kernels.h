@@ -9,8 +9,9 @@ namespace gpo {
 
 struct DonatedTask {
   u64 player, opp;   // position to search, side to move first
-  int alpha, beta;   // window
-  unsigned slot;     // accumulator slot of this task
+  unsigned window;   // alpha & 0xff | (beta & 0xff) << 8 | move from the donor << 16
+  unsigned mbox;     // mailbox index of the donating node
+  unsigned top;      // input position the subtree belongs to
   unsigned pad;
 };
 
@@ -26,23 +27,38 @@ struct BatchedArgs {
   unsigned long long* nodes_out;   // may be null
   DeviceStats* stats;
   unsigned long long node_budget;  // 0 = none
+  int budget_mark;       // 1: an input position over budget gets score -128, no error
   // Frame slots: a node with E empties saves its frame in slot E when it
   // pushes a child.  Slots 2..smem_top live in shared memory, slots
   // smem_top+1..depth in the global array gframes (per-lane, SoA).
   int smem_top;
   unsigned char* gframes;  // (depth - smem_top) * 20 bytes per grid thread, or null
-  // Work donation (splitting hard positions across lanes).  Task slots
-  // 0..n-1 are the input positions; donated subtrees get slots n.. .
-  int donate_min;            // a task root needs this many empties to donate (0 = off)
-  unsigned task_cap;         // donated tasks that fit in the arrays below
-  unsigned* acc;             // per slot: packed (value + 128) << 8 | move, atomicMax
-  unsigned* pending;         // per slot: local search + donated children still running
-  unsigned* parent;          // per donated slot: slot to report to
-  unsigned char* psq;        // per donated slot: move from the parent
-  unsigned* top;             // per donated slot: input position it belongs to
-  DonatedTask* queue;        // donation queue records (task_cap)
-  unsigned* ready;           // per queue record: 1 once written
-  unsigned long long wait_limit_ns;  // bound on an idle lane's wait for work
+  // Work donation (young brothers wait, any depth).  A node whose first
+  // move has returned may hand further moves to idle lanes; results come
+  // back through its mailbox (one per lane and empty count).
+  int donate_min;            // a donating node needs this many empties (0 = off)
+  unsigned long long long_nodes;  // a root past this many nodes hands out moves unasked
+  unsigned* pos_tasks;       // per input position: handed-out subtrees not yet done
+  // Transposition table (table.cuh): 2^tt_bits entries of 16 bytes; nodes
+  // with at least tt_min empties probe it when created and store a bound
+  // when closed.  tt_min = 0 disables it.
+  unsigned long long* tt;
+  int tt_bits;
+  int tt_min;
+  // Learned root orders (mlp.cu): for an input position with at least
+  // learned_min empties, root_lists[pos] replaces the root's ordering
+  // probes (null = off).
+  const u64* root_lists;
+  int learned_min;
+  unsigned max_tasks;        // cap on pos_tasks (bounds the search overhead of splitting)
+  unsigned task_cap;         // queue records (a ring: ticket t uses record t % task_cap)
+  unsigned* mbox_acc;        // [(kMaxEmpties + 1) * grid threads] packed (value+128)<<8 | move
+  unsigned* mbox_pend;       // same shape: handed-out moves not yet reported
+  unsigned* mbox_cancel;     // same shape: 1 = the node was cut off, helpers may stop
+  DonatedTask* queue;        // records, filled in ticket order
+  unsigned* ready;           // per record: ticket + 1 of the last fill
+  unsigned* consumed;        // per record: ticket + 1 of the last read
+  unsigned long long wait_limit_ns;  // deadline of the launch, from its start
 };
 
 struct BatchedLaunch {
@@ -66,5 +82,21 @@ cudaError_t batched_grid(int threads, int smem_top, int sms, int* grid, size_t* 
 // Largest shared-memory frame tier (slots 2..smem_top) that keeps the
 // register-limited occupancy of a `threads`-wide block.
 cudaError_t batched_plan(int threads, int depth, int* smem_top);
+
+// Learned orderer (mlp.cu).
+bool mlp_loaded();
+int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
+                    u64* d_lists, cudaStream_t s);
+
+// Positions whose score is -128 (over budget in a first pass), compacted:
+// idx[0..*count) = their indices, in order.
+cudaError_t launch_collect_marked(const signed char* score, int n, unsigned* idx, unsigned* count,
+                                  cudaStream_t s);
+cudaError_t launch_gather(const u64* P, const u64* O, const unsigned* idx, int count, u64* outP,
+                          u64* outO, cudaStream_t s);
+cudaError_t launch_scatter_scores(const signed char* sc, const signed char* best,
+                                  const unsigned long long* nodes, const unsigned* idx, int count,
+                                  signed char* score_out, signed char* best_out,
+                                  unsigned long long* nodes_out, cudaStream_t s);
 
 }  // namespace gpo

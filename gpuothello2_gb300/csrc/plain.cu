@@ -36,7 +36,8 @@ struct PlainUpper {
 };
 
 // Legal moves of an upper node in the reference's order.
-__device__ __forceinline__ int plain_upper_moves(u64 P, u64 O, unsigned char* list) {
+__device__ __forceinline__ int plain_upper_moves(u64 P, u64 O, unsigned char* list,
+                                                 const u64* rays) {
   unsigned char key[kMaxEmpties];
   int n = 0;
   const u64 moves = gpo_mobility(P, O);
@@ -46,7 +47,7 @@ __device__ __forceinline__ int plain_upper_moves(u64 P, u64 O, unsigned char* li
       const int sq = ctz64(m);
       m &= m - 1;
       const u64 bit = 1ULL << sq;
-      const u64 f = gpo_flip(P, O, sq);
+      const u64 f = gpo_flip(P, O, sq, rays);
       const int k = popc(gpo_mobility(O ^ f, P ^ f ^ bit));
       int j = n++;
       while (j > 0 && key[j - 1] > k) {
@@ -74,7 +75,10 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
   __shared__ u64 sO[kPlainLower][kPlainBlock];
   __shared__ u64 sM[kPlainLower][kPlainBlock];
   __shared__ int sMeta[kPlainLower][kPlainBlock];
+  __shared__ __align__(16) u64 rays[256];
   PlainUpper up[kMaxEmpties - 8];
+  gpo_build_rays(rays);
+  __syncthreads();
 
   const int t = threadIdx.x;
   const int i = blockIdx.x * blockDim.x + t;
@@ -91,7 +95,7 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
       int level = 0;
       int alpha = -64, beta = 64, result = -64, passed = 0, found = 0, idx = 0, cnt = 0;
       u64 moves = 0;
-      cnt = plain_upper_moves(P, O, up[0].list);
+      cnt = plain_upper_moves(P, O, up[0].list, rays);
       nodes = 1;
       for (;;) {
         // Each pass either pushes a child / passes in place (continue) or
@@ -111,7 +115,7 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
                 result = -64;
                 passed = 1;
                 ++nodes;
-                cnt = plain_upper_moves(P, O, up[level].list);
+                cnt = plain_upper_moves(P, O, up[level].list, rays);
                 idx = 0;
                 continue;
               }
@@ -119,7 +123,7 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
           } else if (alpha < beta) {
             const int sq = up[level].list[idx++];
             const u64 bit = 1ULL << sq;
-            const u64 f = gpo_flip(P, O, sq);
+            const u64 f = gpo_flip(P, O, sq, rays);
             PlainUpper& fr = up[level];
             fr.P = P; fr.O = O; fr.alpha = alpha; fr.beta = beta; fr.result = result;
             fr.idx = idx; fr.n = cnt; fr.passed = passed;
@@ -134,7 +138,7 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
             if (level < U) {
               result = -64;
               idx = 0;
-              cnt = plain_upper_moves(P, O, up[level].list);
+              cnt = plain_upper_moves(P, O, up[level].list, rays);
             } else {
               result = -127;
               found = 0;
@@ -166,7 +170,7 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
             moves ^= bit;
             found = 1;
             const int sq = ctz64(bit);
-            const u64 f = gpo_flip(P, O, sq);
+            const u64 f = gpo_flip(P, O, sq, rays);
             const int l = level - U;
             if (l >= kPlainLower) {  // depth >= empties makes this unreachable
               atomicOr(&stats->status, kErrInternal);

@@ -105,6 +105,9 @@ struct Xoshiro {
 
 __global__ void generate_kernel(u64 seed, u64 first, int n, int min_e, int max_e,
                                 u64* __restrict__ out_p, u64* __restrict__ out_o) {
+  __shared__ __align__(16) u64 rays[256];
+  gpo_build_rays(rays);
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const u64 black0 = 0x0000000810000000ULL, white0 = 0x0000001008000000ULL;
@@ -137,7 +140,7 @@ __global__ void generate_kernel(u64 seed, u64 first, int n, int min_e, int max_e
     u64 j = r.uniform(static_cast<u64>(popc(moves)));
     while (j--) moves &= moves - 1;
     const int sq = ctz64(moves);
-    const u64 f = gpo_flip(P, O, sq);
+    const u64 f = gpo_flip(P, O, sq, rays);
     const u64 nP = O ^ f, nO = P ^ f ^ (1ULL << sq);
     P = nP;
     O = nO;
@@ -159,6 +162,81 @@ cudaError_t launch_bucket(const u64* player, const u64* opp, int n, int depth, u
 cudaError_t launch_generate(u64 seed, u64 first, int n, int min_e, int max_e, u64* out_p,
                             u64* out_o, cudaStream_t s) {
   generate_kernel<<<(n + 127) / 128, 128, 0, s>>>(seed, first, n, min_e, max_e, out_p, out_o);
+  return cudaGetLastError();
+}
+
+// ---- second pass of hard positions ----
+__global__ void collect_marked_kernel(const signed char* __restrict__ score, int n,
+                                      unsigned* __restrict__ idx, unsigned* __restrict__ count) {
+  // one block: keeps the marked indices in ascending order
+  __shared__ unsigned base;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  for (int start = 0; start < n; start += blockDim.x) {
+    const int i = start + threadIdx.x;
+    const bool m = i < n && score[i] == -128;
+    const unsigned ballot = __ballot_sync(0xffffffffu, m);
+    __shared__ unsigned warp_cnt[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_cnt[warp] = __popc(ballot);
+    __syncthreads();
+    unsigned off = base;
+    for (int w = 0; w < warp; ++w) off += warp_cnt[w];
+    if (m) idx[off + __popc(ballot & ((1u << lane) - 1u))] = static_cast<unsigned>(i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned total = 0;
+      for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) total += warp_cnt[w];
+      base += total;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = base;
+}
+
+__global__ void gather_kernel(const u64* __restrict__ P, const u64* __restrict__ O,
+                              const unsigned* __restrict__ idx, int count, u64* __restrict__ outP,
+                              u64* __restrict__ outO) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) {
+    outP[i] = P[idx[i]];
+    outO[i] = O[idx[i]];
+  }
+}
+
+__global__ void scatter_scores_kernel(const signed char* __restrict__ sc,
+                                      const signed char* __restrict__ best,
+                                      const unsigned long long* __restrict__ nodes,
+                                      const unsigned* __restrict__ idx, int count,
+                                      signed char* __restrict__ score_out,
+                                      signed char* __restrict__ best_out,
+                                      unsigned long long* __restrict__ nodes_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) {
+    score_out[idx[i]] = sc[i];
+    if (best_out) best_out[idx[i]] = best[i];
+    if (nodes_out) nodes_out[idx[i]] += nodes[i];
+  }
+}
+
+cudaError_t launch_collect_marked(const signed char* score, int n, unsigned* idx, unsigned* count,
+                                  cudaStream_t s) {
+  collect_marked_kernel<<<1, 1024, 0, s>>>(score, n, idx, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const u64* P, const u64* O, const unsigned* idx, int count, u64* outP,
+                          u64* outO, cudaStream_t s) {
+  gather_kernel<<<(count + 255) / 256, 256, 0, s>>>(P, O, idx, count, outP, outO);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_scores(const signed char* sc, const signed char* best,
+                                  const unsigned long long* nodes, const unsigned* idx, int count,
+                                  signed char* score_out, signed char* best_out,
+                                  unsigned long long* nodes_out, cudaStream_t s) {
+  scatter_scores_kernel<<<(count + 255) / 256, 256, 0, s>>>(sc, best, nodes, idx, count, score_out,
+                                                            best_out, nodes_out);
   return cudaGetLastError();
 }
 

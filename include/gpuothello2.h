@@ -40,7 +40,7 @@ extern "C" {
 #define GPO_ERR_BOARD (-3)    /* a square is set in both bitboards */
 #define GPO_ERR_CUDA (-4)     /* CUDA runtime error (no device, launch failure, ...) */
 #define GPO_ERR_NOMEM (-5)    /* device or pinned-host allocation failed */
-#define GPO_ERR_TIMEOUT (-6)  /* a search exceeded gpo_options.node_budget */
+#define GPO_ERR_TIMEOUT (-6)  /* node_budget exceeded, or the search passed wait_limit_ms */
 #define GPO_ERR_INTERNAL (-7) /* a kernel consistency check failed */
 #define GPO_ERR_IO (-8)       /* file could not be read or written */
 
@@ -55,15 +55,21 @@ extern "C" {
 
 typedef struct gpo_options {
   int method;                 /* GPO_METHOD_* */
-  int use_table;              /* transposition table: -1 auto, 0 off, 1 on */
-  int use_learned;            /* learned move ordering: -1 auto, 0 off, 1 on */
+  int use_table;              /* transposition table: 1 on; 0 or -1 (auto) off; cleared at
+                                 every call, so no result carries over */
+  int use_learned;            /* learned root ordering (gpo_mlp_load): -1 auto (on when a
+                                 network is loaded), 0 off, 1 on */
   int threads_per_block;      /* 0 = tuned default */
   int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties; 0 = tuned */
-  int learned_min_empties;    /* learned ordering at nodes with >= this many empties; 0 = 14 */
+  int learned_min_empties;    /* learned ordering at roots with >= this many empties; 0 = 14 */
   uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog) */
-  int split_min_empties;      /* hard positions are split across lanes from this many
-                                 empties; 0 = tuned default, negative = never split */
-  int wait_limit_ms;          /* bound on an idle lane's wait for split work; 0 = 120000 */
+  int split_min_empties;      /* hard positions (over 2^22 nodes in a first pass) are solved
+                                 again with their subtrees split across idle lanes, from
+                                 nodes with this many empties; 0 = 12, negative = never */
+  int wait_limit_ms;          /* deadline of one search launch (a watchdog on waits between
+                                 lanes); 0 = 600000 */
+  int table_bits;             /* transposition table of 2^table_bits 16-byte entries; 0 = 24 */
+  int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 11 */
 } gpo_options;
 
 typedef struct gpo_stats {
@@ -124,6 +130,27 @@ int gpo_generate(uint64_t seed, uint64_t first, int n, int min_empties, int max_
                  uint64_t* player, uint64_t* opp);
 int gpo_generate_device(uint64_t seed, uint64_t first, int n, int min_empties, int max_empties,
                         uint64_t* d_player, uint64_t* d_opp, void* stream);
+
+
+/*
+ * Learned move orderer (no counterpart in the reference: the north-star's
+ * learned part).  An MLP 192 -> 256 -> 256 -> 64 over (side-to-move discs,
+ * other discs, legal moves) with BF16 tensor-core products and FP32
+ * accumulation, trained on the GPU on best-move labels from
+ * solve_batch_ex.  Weights are a flat FP32 array of gpo_mlp_param_count()
+ * values: W1[192][256], b1[256], W2[256][256], b2[256], W3[256][64], b3[64].
+ * gpo_mlp_load makes the solver order the root moves of positions with
+ * >= learned_min_empties empties by the network (scores stay exact).
+ */
+int gpo_mlp_param_count(void);
+int gpo_mlp_init(uint64_t seed, float* weights);
+int gpo_mlp_forward(const float* weights, const uint64_t* player, const uint64_t* opp, int n,
+                    float* logits);
+int gpo_mlp_gradients(const float* weights, const uint64_t* player, const uint64_t* opp,
+                      const int8_t* best, int n, float* grads, float* loss);
+int gpo_mlp_train(const uint64_t* player, const uint64_t* opp, const int8_t* best, int n,
+                  int epochs, int batch, float lr, uint64_t seed, float* weights, float* history);
+int gpo_mlp_load(const float* weights);
 
 /* Releases the library context (device buffers, table, stream). */
 void solve_shutdown(void);

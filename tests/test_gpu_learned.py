@@ -1,0 +1,91 @@
+"""Learned move orderer on the GPU: forward and gradients against the CPU
+reference (tests/mlp_ref.py), training on solver-made labels, and its use in
+the solver (exact scores, node counts reported)."""
+import numpy as np
+import pytest
+
+from tests import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def labelled(gpu, seed, n, lo, hi):
+    p, o = gpu.generate(seed, n, lo, hi)
+    _, best, _, _, _ = gpu.solve(p, o, hi, best=True)
+    return p, o, best
+
+
+def legal_of(oracle, p, o):
+    return np.array([oracle.L.orc_mobility(int(a), int(b)) for a, b in zip(p, o)], np.uint64)
+
+
+def test_forward_matches_reference(gpu, oracle):
+    w = gpu.mlp_init(7)
+    p, o = oracle.generate(3, 96, 12, 14)
+    z = gpu.mlp_forward(w, p, o)
+    X = mlp_ref.features(p, o, legal_of(oracle, p, o))
+    _, _, zr = mlp_ref.forward(w, X)
+    # BF16 products, FP32 accumulation in a different order: tolerance 2%
+    # of the logit scale
+    scale = np.abs(zr).max()
+    assert np.abs(z - zr).max() <= 2e-2 * scale
+
+
+def test_gradients_match_reference(gpu, oracle):
+    w = gpu.mlp_init(11)
+    p, o, best = labelled(gpu, 3, 128, 12, 14)
+    g, loss = gpu.mlp_gradients(w, p, o, best)
+    legal = legal_of(oracle, p, o)
+    X = mlp_ref.features(p, o, legal)
+    lr, gr = mlp_ref.loss_and_gradients(w, X, legal, best.astype(int))
+    assert abs(loss - lr) <= 1e-2 * abs(lr)
+    # per parameter block: relative L2 error within 5% (BF16 deltas)
+    off = 0
+    for name, shape in mlp_ref.SHAPES:
+        size = int(np.prod(shape))
+        a, b = g[off:off + size], gr[off:off + size]
+        assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b) + 1e-7, name
+        off += size
+
+
+def test_training_learns_best_moves(gpu, oracle):
+    p, o, best = labelled(gpu, 3, 65536, 12, 14)
+    w0 = gpu.mlp_init(3)
+    w, hist = gpu.mlp_train(p, o, best, w0, epochs=4, batch=2048, lr=1e-3, seed=1)
+    losses = [h[0] for h in hist]
+    assert losses[-1] < losses[0]
+    # held-out positions: top-1 agreement with the solver's best move beats
+    # the untrained network clearly
+    q, r, qb = labelled(gpu, 33, 4096, 12, 14)
+    legal = legal_of(oracle, q, r)
+
+    def top1(weights):
+        z = gpu.mlp_forward(weights, q, r)
+        hits = n = 0
+        for i in range(len(q)):
+            m = [k for k in range(64) if (int(legal[i]) >> k) & 1]
+            if not m or qb[i] >= 64:
+                continue
+            n += 1
+            hits += m[int(np.argmax(z[i, m]))] == qb[i]
+        return hits / n
+
+    acc0, acc1 = top1(w0), top1(w)
+    print("best-move top-1: untrained %.3f trained %.3f" % (acc0, acc1))
+    assert acc1 > acc0 + 0.1
+
+
+def test_learned_root_order_keeps_scores_exact(gpu):
+    p, o, best = labelled(gpu, 3, 32768, 12, 14)
+    w, _ = gpu.mlp_train(p, o, best, gpu.mlp_init(5), epochs=3, batch=2048, lr=1e-3, seed=2)
+    q, r = gpu.generate(4, 2048, 14, 16)
+    s0, _, _, st0, _ = gpu.solve(q, r, 16, use_learned=0, split_min_empties=-1)
+    gpu.mlp_load(w)
+    try:
+        s1, _, _, st1, _ = gpu.solve(q, r, 16, use_learned=1, split_min_empties=-1)
+    finally:
+        gpu.mlp_load(None)
+    assert np.array_equal(s0, s1)
+    assert st1.learned_calls == len(q)
+    print("nodes: fastest-first roots %d, learned roots %d (%.3f)" %
+          (st0.nodes, st1.nodes, st1.nodes / st0.nodes))

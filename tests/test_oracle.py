@@ -76,7 +76,7 @@ def test_oracle_reference_tree_matches_reference(oracle, name, seed, count, lo, 
     oracle walks the reference's exact tree."""
     p, o, scores, steps = golden_ref(name)
     if name.startswith("c5"):
-        pytest.skip("20-22 empties in reference order take minutes on the CPU; covered by the fast solver")
+        pytest.skip("20-22 empties in reference order take minutes on the CPU; the GPU tests check these scores")
     sc, st, _, _ = oracle.solve_batch(p, o, depth, mode=0)
     assert np.array_equal(sc.astype(int), scores)
     assert np.array_equal(st, steps)
