@@ -30,7 +30,7 @@ METHOD_PLAIN = 1
 EXPORTED_SYMBOLS = (
     "gpo_default_options", "solve_batch", "solve_batch_ex", "solve_batch_device",
     "gpo_generate", "gpo_generate_device", "solve_shutdown", "gpo_strerror",
-    "gpo_device_info", "gpo_mlp_param_count", "gpo_mlp_init",
+    "gpo_device_info", "solve_batch_device_noalloc", "gpo_mlp_param_count", "gpo_mlp_init",
     "gpo_mlp_forward", "gpo_mlp_gradients", "gpo_mlp_train", "gpo_mlp_load",
 )
 
@@ -98,6 +98,7 @@ def lib():
         L.gpo_strerror.argtypes = [i]
         L.gpo_strerror.restype = ctypes.c_char_p
         L.gpo_device_info.argtypes = [ctypes.c_char_p, i, ctypes.POINTER(ctypes.c_int)]
+        L.solve_batch_device_noalloc.argtypes = [vp, vp, i, i, vp, vp]
         f32 = ctypes.c_float
         L.gpo_mlp_param_count.argtypes = []
         L.gpo_mlp_init.argtypes = [u64, vp]

@@ -36,7 +36,7 @@ NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 
-CU_SOURCES = ["plain.cu", "batched.cu", "prep.cu", "capi.cu", "mlp.cu"]
+CU_SOURCES = ["plain.cu", "batched.cu", "prep.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
 INTPEAK_LIB = os.path.join(LIB_DIR, "libgpo_intpeak.so")
 
 

@@ -131,6 +131,24 @@ int gpo_generate(uint64_t seed, uint64_t first, int n, int min_empties, int max_
 int gpo_generate_device(uint64_t seed, uint64_t first, int n, int min_empties, int max_empties,
                         uint64_t* d_player, uint64_t* d_opp, void* stream);
 
+/*
+ * No counterpart in the reference.  The batched solver for callers that
+ * cannot allocate device memory (a host program whose pool allocator owns
+ * all device memory, a plugin that may not allocate after start-up, code that
+ * must avoid the device synchronisation an allocation can cause).  It
+ * allocates nothing: its scratch lives in a fixed array inside the library
+ * (about 12 MiB, held by every GPU that loads the library until exit).
+ * Device input and score arrays as in solve_batch_device; `stream` may be
+ * NULL (the legacy default stream).  At most GPO_NOALLOC_MAX_POSITIONS
+ * positions (else GPO_ERR_ARG) and depth <= GPO_NOALLOC_MAX_DEPTH (else
+ * GPO_ERR_DEPTH).  Splitting and the transposition table are off.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.
+ */
+#define GPO_NOALLOC_MAX_POSITIONS (1 << 20)
+#define GPO_NOALLOC_MAX_DEPTH 16
+int solve_batch_device_noalloc(const uint64_t* d_player, const uint64_t* d_opp, int n, int depth,
+                               int8_t* d_score, void* stream);
 
 /*
  * Learned move orderer (no counterpart in the reference: the north-star's
