@@ -19,7 +19,7 @@ the timed region.
   roofline  integer-ALU bound: 418 INT32 ops per node (mobility + flip +
          make-move of the reference arithmetic) x nodes / batched-kernel
          time, against the INT32 issue rate measured live by
-         libgpo_intpeak.so (MEASURED_PEAKS.json has no integer peak)
+         libgpo_intpeak.so (the HBM and BF16 peaks do not bound integer code)
   cpu_baseline  the oracle's restatement of the reference tree on all host
          cores, on a bounded sample of the same stream
 
@@ -42,6 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W_NODE = 418  # INT32 ops per node: mobility + flip + make-move of the reference arithmetic
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per position of
+# one batched-kernel launch, from one ncu capture of a 131,072-position launch
+# (2,711,552 B), scaled to the launch by its position count.
+DRAM_BYTES_PER_POSITION = 2711552.0 / 131072
 SEED, N_POS, LO, HI, DEPTH = 2, 1 << 20, 8, 16, 16
 METRIC = "exact-solved positions/s at 8-16 empties (batched vs plain, same GB300)"
 WORKLOAD = ("1,048,576 positions, random playouts seed 2, empties uniform 8..16, DEPTH 16")
@@ -320,7 +324,9 @@ def main():
                 "d2h_bytes_per_step": n,
                 "how": "last warm-up step through solve_batch_ex, pinned host buffers, wall clock"},
         "roofline": {"bound": "int32-alu", "achieved": achieved / 1e12, "peak": int_peak / 1e12,
-                     "unit": "TOPS (INT32)", "frac": achieved / int_peak, "traffic": None,
+                     "unit": "TOPS (INT32)", "frac": achieved / int_peak,
+                     "traffic": DRAM_BYTES_PER_POSITION * n,
+                     "traffic_source": "ncu capture of 131,072 positions scaled by positions",
                      "peak_source": "measured live: lop3.b32/add.u32 issue rate (libgpo_intpeak)",
                      "kernel": "batched_kernel", "ops_per_node": W_NODE,
                      "nodes_per_launch": mean_nodes, "kernel_ms": 1000.0 * mean_kern_s},

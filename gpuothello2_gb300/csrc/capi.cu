@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "../../include/gpuothello2.h"
 #include "kernels.h"
@@ -202,8 +203,9 @@ int check_options(const gpo_options* opt) {
   if (!opt) return GPO_OK;
   if (opt->table_bits != 0 && (opt->table_bits < 16 || opt->table_bits > 31)) return GPO_ERR_ARG;
   if (opt->method != GPO_METHOD_BATCHED && opt->method != GPO_METHOD_PLAIN) return GPO_ERR_ARG;
+  // the batched kernel is compiled for at most 256 threads per block
   if (opt->threads_per_block != 0 &&
-      (opt->threads_per_block < 32 || opt->threads_per_block > 1024 || opt->threads_per_block % 32))
+      (opt->threads_per_block < 32 || opt->threads_per_block > 256 || opt->threads_per_block % 32))
     return GPO_ERR_ARG;
   return GPO_OK;
 }
@@ -338,6 +340,126 @@ int ensure_second(Context* c, size_t n) {
   return GPO_OK;
 }
 
+// One level of the expansion: positions, their results, and (below the
+// input level) their parent and move.
+struct Level {
+  const u64* P = nullptr;
+  const u64* O = nullptr;
+  signed char* score = nullptr;
+  signed char* best = nullptr;
+  unsigned long long* nodes = nullptr;
+  unsigned* parent = nullptr;
+  unsigned char* move = nullptr;
+  int n = 0;
+  unsigned* idx = nullptr;  // marked (over budget) positions of this level
+  int m = 0;
+  unsigned* acc = nullptr;
+  std::vector<void*> owned;
+  ~Level() {
+    for (void* p : owned) cudaFree(p);
+  }
+  template <class T>
+  cudaError_t alloc(T** p, size_t count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e == cudaSuccess) owned.push_back(*p);
+    return e;
+  }
+};
+
+constexpr int kExpandLevels = 6;
+constexpr unsigned long long kLevelBudget = 1ULL << 22;
+
+// Hard positions (over kLevelBudget nodes) are replaced by their children,
+// solved as independent positions in the next pass (again with the budget,
+// except in the last level); values combine bottom-up as the max of the
+// children's negated exact scores.  No lane ever waits for another, and
+// every child is an ordinary full-window solve, so a hard position spreads
+// over 10x, 100x, ... lanes without the stale-window cost of splitting a
+// running search.
+int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
+                 gpo_stats* stats, cudaStream_t s) {
+  Level lv[kExpandLevels];
+  lv[0].P = dP;
+  lv[0].O = dO;
+  lv[0].score = dScore;
+  lv[0].best = dBest;
+  lv[0].nodes = dNodes;
+  lv[0].n = n;
+  unsigned long long nodes = 0, probes = 0, hits = 0, updates = 0, learned = 0;
+  double ms = 0.0;
+  int rc = GPO_OK;
+  int last = 0;
+  for (int k = 0; k < kExpandLevels; ++k) {
+    Level& L = lv[k];
+    const bool final_level = k == kExpandLevels - 1;
+    PassConfig pc;
+    pc.budget = final_level ? 0 : kLevelBudget;
+    pc.mark = !final_level;
+    pc.split = false;
+    pc.clear_table = k == 0;
+    PassResult r;
+    rc = run_pass(c, L.P, L.O, L.n, depth, L.score, L.best, L.nodes, o, pc, s, &r);
+    nodes += r.hs.nodes;
+    probes += r.hs.tt_probes;
+    hits += r.hs.tt_hits;
+    updates += r.hs.tt_updates;
+    learned += r.learned;
+    ms += r.ms;
+    last = k;
+    if (rc != GPO_OK || final_level) break;
+    // over-budget positions of this level
+    GPO_CK(L.alloc(&L.idx, static_cast<size_t>(L.n)));
+    GPO_CK(launch_collect_marked(L.score, L.n, L.idx, c->dCursor, s));
+    unsigned m = 0;
+    GPO_CK(cudaMemcpyAsync(&m, c->dCursor, sizeof(m), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    L.m = static_cast<int>(m);
+    if (m == 0) break;
+    // their children form the next level
+    Level& C = lv[k + 1];
+    const size_t cap = static_cast<size_t>(m) * 33;
+    u64 *cP = nullptr, *cO = nullptr;
+    GPO_CK(C.alloc(&cP, cap));
+    GPO_CK(C.alloc(&cO, cap));
+    GPO_CK(C.alloc(&C.parent, cap));
+    GPO_CK(C.alloc(&C.move, cap));
+    GPO_CK(C.alloc(&C.score, cap));
+    if (L.nodes) GPO_CK(C.alloc(&C.nodes, cap));
+    GPO_CK(cudaMemsetAsync(c->dCursor + 1, 0, sizeof(unsigned), s));
+    GPO_CK(launch_expand(L.P, L.O, L.idx, L.m, cP, cO, C.parent, C.move, c->dCursor + 1,
+                         static_cast<unsigned>(cap), s));
+    unsigned cn = 0;
+    GPO_CK(cudaMemcpyAsync(&cn, c->dCursor + 1, sizeof(cn), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    if (cn > cap) return GPO_ERR_INTERNAL;
+    C.P = cP;
+    C.O = cO;
+    C.n = static_cast<int>(cn);
+  }
+  // combine from the deepest level up
+  for (int k = last; k >= 1 && rc == GPO_OK; --k) {
+    Level& C = lv[k];
+    Level& L = lv[k - 1];
+    GPO_CK(L.alloc(&L.acc, static_cast<size_t>(L.n)));
+    GPO_CK(cudaMemsetAsync(L.acc, 0, static_cast<size_t>(L.n) * sizeof(unsigned), s));
+    GPO_CK(launch_combine(C.score, C.parent, C.move, C.nodes, C.n, L.acc, L.nodes, s));
+    GPO_CK(launch_finalize(L.idx, L.m, L.acc, L.score, L.best, s));
+  }
+  GPO_CK(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->nodes = nodes;
+    stats->table_probes = probes;
+    stats->table_hits = hits;
+    stats->table_updates = updates;
+    stats->learned_calls = learned;
+    stats->splits = 0;
+    for (int k = 1; k <= last; ++k) stats->splits += static_cast<unsigned long long>(lv[k].n);
+    stats->kernel_ms = ms;
+  }
+  return rc;
+}
+
 // Runs the solve pipeline on device arrays already in place.  Batched
 // method: a first pass gives every position a node budget; the few hard
 // positions that exceed it are solved again in a second pass in which idle
@@ -365,7 +487,11 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
     }
     return status_to_error(hs.status);
   }
-  const bool split = o.split_min_empties >= 0;
+  // split_min_empties: 0 (default) = expand hard positions into their
+  // children level by level; > 0 = hand subtrees of hard positions to idle
+  // lanes inside the kernel (second pass); < 0 = one pass, no splitting.
+  if (o.split_min_empties == 0 && o.node_budget == 0) return run_expanded(c, dP, dO, n, depth, dScore, dBest, dNodes, o, stats, s);
+  const bool split = o.split_min_empties > 0;
   const bool two_pass = split && o.node_budget == 0;
   PassConfig p1;
   p1.budget = two_pass ? (1ULL << 22) : o.node_budget;

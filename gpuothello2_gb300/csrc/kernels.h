@@ -99,4 +99,15 @@ cudaError_t launch_scatter_scores(const signed char* sc, const signed char* best
                                   signed char* score_out, signed char* best_out,
                                   unsigned long long* nodes_out, cudaStream_t s);
 
+// Expansion of hard positions into their children and the bottom-up
+// combination of the children's exact scores (prep.cu).
+cudaError_t launch_expand(const u64* P, const u64* O, const unsigned* idx, int m, u64* cP, u64* cO,
+                          unsigned* cparent, unsigned char* cmove, unsigned* counter, unsigned cap,
+                          cudaStream_t s);
+cudaError_t launch_combine(const signed char* cscore, const unsigned* cparent,
+                           const unsigned char* cmove, const unsigned long long* cnodes, int count,
+                           unsigned* acc, unsigned long long* nodes, cudaStream_t s);
+cudaError_t launch_finalize(const unsigned* idx, int m, const unsigned* acc, signed char* score,
+                            signed char* best, cudaStream_t s);
+
 }  // namespace gpo

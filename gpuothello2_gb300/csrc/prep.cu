@@ -240,4 +240,89 @@ cudaError_t launch_scatter_scores(const signed char* sc, const signed char* best
   return cudaGetLastError();
 }
 
+// ---- expansion of hard positions into their children ----
+// For each marked position idx[i] of a level: its children (after each
+// legal move, or the swapped position when it must pass) are appended to the
+// next level, with the parent's index and the move (64 = pass).
+__global__ void expand_kernel(const u64* __restrict__ P, const u64* __restrict__ O,
+                              const unsigned* __restrict__ idx, int m, u64* __restrict__ cP,
+                              u64* __restrict__ cO, unsigned* __restrict__ cparent,
+                              unsigned char* __restrict__ cmove, unsigned* __restrict__ counter,
+                              unsigned cap) {
+  __shared__ __align__(16) u64 rays[256];
+  gpo_build_rays(rays);
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const unsigned j = idx[i];
+  const u64 p = P[j], o = O[j];
+  u64 moves = gpo_mobility(p, o);
+  const int cnt = moves ? popc(moves) : 1;
+  const unsigned base = atomicAdd(counter, static_cast<unsigned>(cnt));
+  if (base + cnt > cap) return;  // the host checks the counter against cap
+  if (!moves) {
+    cP[base] = o;
+    cO[base] = p;
+    cparent[base] = j;
+    cmove[base] = static_cast<unsigned char>(kMovePassDev);
+    return;
+  }
+  for (int k = 0; moves; ++k) {
+    const u64 bit = moves & (0ULL - moves);
+    moves ^= bit;
+    const int sq = ctz64(bit);
+    const u64 f = gpo_flip(p, o, sq, rays);
+    cP[base + k] = o ^ f;
+    cO[base + k] = p ^ f ^ bit;
+    cparent[base + k] = j;
+    cmove[base + k] = static_cast<unsigned char>(sq);
+  }
+}
+
+// acc[parent] = max over children of (-score) packed with the move;
+// node counts of children are added to their parent's.
+__global__ void combine_kernel(const signed char* __restrict__ cscore,
+                               const unsigned* __restrict__ cparent,
+                               const unsigned char* __restrict__ cmove,
+                               const unsigned long long* __restrict__ cnodes, int count,
+                               unsigned* __restrict__ acc, unsigned long long* __restrict__ nodes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int v = -static_cast<int>(cscore[i]);
+  atomicMax(&acc[cparent[i]], (static_cast<unsigned>(v + 128) << 8) | cmove[i]);
+  if (nodes && cnodes) atomicAdd(&nodes[cparent[i]], cnodes[i]);
+}
+
+__global__ void finalize_kernel(const unsigned* __restrict__ idx, int m,
+                                const unsigned* __restrict__ acc, signed char* __restrict__ score,
+                                signed char* __restrict__ best) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const unsigned a = acc[idx[i]];
+  score[idx[i]] = static_cast<signed char>(static_cast<int>(a >> 8) - 128);
+  if (best) best[idx[i]] = static_cast<signed char>(a & 255u);
+}
+
+cudaError_t launch_expand(const u64* P, const u64* O, const unsigned* idx, int m, u64* cP, u64* cO,
+                          unsigned* cparent, unsigned char* cmove, unsigned* counter, unsigned cap,
+                          cudaStream_t s) {
+  expand_kernel<<<(m + 127) / 128, 128, 0, s>>>(P, O, idx, m, cP, cO, cparent, cmove, counter,
+                                                 cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_combine(const signed char* cscore, const unsigned* cparent,
+                           const unsigned char* cmove, const unsigned long long* cnodes, int count,
+                           unsigned* acc, unsigned long long* nodes, cudaStream_t s) {
+  combine_kernel<<<(count + 255) / 256, 256, 0, s>>>(cscore, cparent, cmove, cnodes, count, acc,
+                                                     nodes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const unsigned* idx, int m, const unsigned* acc, signed char* score,
+                            signed char* best, cudaStream_t s) {
+  finalize_kernel<<<(m + 255) / 256, 256, 0, s>>>(idx, m, acc, score, best);
+  return cudaGetLastError();
+}
+
 }  // namespace gpo

@@ -59,7 +59,7 @@ typedef struct gpo_options {
                                  every call, so no result carries over */
   int use_learned;            /* learned root ordering (gpo_mlp_load): -1 auto (on when a
                                  network is loaded), 0 off, 1 on */
-  int threads_per_block;      /* 0 = tuned default */
+  int threads_per_block;      /* 32..256, multiple of 32; 0 = 128 */
   int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties; 0 = tuned */
   int learned_min_empties;    /* learned ordering at roots with >= this many empties; 0 = 14 */
   uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog) */
