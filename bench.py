@@ -251,7 +251,7 @@ def main():
                 solve_device(method)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(steps)]
-        kern_ms, nodes, splits = [], [], []
+        kern_ms, nodes, splits, launches = [], [], [], []
         barrier()
         if sampler:
             sampler.__enter__()
@@ -263,16 +263,19 @@ def main():
             kern_ms.append(st.kernel_ms)
             nodes.append(st.nodes)
             splits.append(st.splits)
+            launches.append(st.launches)
         barrier()
         if sampler:
             sampler.__exit__(None, None, None)
         step_ms = [a.elapsed_time(b) for a, b in ev]
         timed.splits = splits
+        timed.launches = launches
         return step_ms, kern_ms, nodes
 
     sampler = ClockSampler(local)
     e2e_t = []
     step_ms, kern_ms, nodes = timed(g.METHOD_BATCHED, args.warmup, args.steps, sampler, e2e_t)
+    batched_splits, batched_launches = list(timed.splits), int(sum(timed.launches))
     total_s = sum(step_ms) / 1000.0
     if world > 1:
         t = torch.tensor([total_s], device=dev, dtype=torch.float64)
@@ -311,7 +314,6 @@ def main():
                "sample": "first %d positions of the workload stream (%.1f s), oracle "
                          "restatement of the reference tree, %d threads" % (done, dt, thr)}
 
-    launches_per_step = 4  # bucket count, bucket scan, bucket scatter, batched search
     line = {
         "metric": METRIC, "value": value, "unit": "positions/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
@@ -331,10 +333,12 @@ def main():
                      "kernel": "batched_kernel", "ops_per_node": W_NODE,
                      "nodes_per_launch": mean_nodes, "kernel_ms": 1000.0 * mean_kern_s},
         "nodes_per_s": mean_nodes / mean_kern_s,
-        "splits_per_step": statistics.mean(timed.splits) if timed.splits else 0,
+        "splits_per_step": statistics.mean(batched_splits) if batched_splits else 0,
         "cpu_baseline": cpu,
         "clocks": sampler.summary(),
-        "gpu_launches": launches_per_step * args.steps,
+        # counted by the library per call: bucketing (3) and the search per
+        # pass, plus marking, expansion and combination kernels per level
+        "gpu_launches": batched_launches,
         "plain": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
     }

@@ -61,6 +61,7 @@ class Stats(ctypes.Structure):
         ("splits", ctypes.c_uint64),
         ("kernel_ms", ctypes.c_double),
         ("total_ms", ctypes.c_double),
+        ("launches", ctypes.c_uint64),
     ]
 
     def as_dict(self):

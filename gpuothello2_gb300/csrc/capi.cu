@@ -57,6 +57,7 @@ struct Context {
   signed char* d2Score = nullptr;
   signed char* d2Best = nullptr;
   unsigned long long* d2Nodes = nullptr;
+  unsigned long long launches = 0;  // kernels launched since the context was made
 };
 
 constexpr unsigned kTaskCap = 1u << 20;  // queue records (a ring, reused within a call)
@@ -231,6 +232,7 @@ int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed 
   GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
   GPO_CK(cudaMemsetAsync(c->dHist, 0, 65 * sizeof(unsigned), s));
   GPO_CK(launch_bucket(dP, dO, n, depth, c->dHist, c->dCursor, c->dPerm, c->dStats, c->sms, s));
+  c->launches += 3;
   // Learned root orders for the positions with >= learned_min empties
   // (the front of the bucketed queue).
   const int lmin = o.learned_min_empties > 0 ? o.learned_min_empties : 14;
@@ -243,7 +245,9 @@ int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed 
     GPO_CK(cudaStreamSynchronize(s));
     for (int e = lmin; e <= 64; ++e) learned_count += hist[e];
     if (learned_count > 0) {
-      const int rcl = mlp_order_roots(dP, dO, c->dPerm, learned_count, c->dLists, s);
+      unsigned launched = 0;
+      const int rcl = mlp_order_roots(dP, dO, c->dPerm, learned_count, c->dLists, s, &launched);
+      c->launches += launched;
       if (rcl != GPO_OK) return rcl;
       pr->learned = static_cast<unsigned long long>(learned_count);
     }
@@ -314,6 +318,7 @@ int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed 
   if (dNodes) GPO_CK(cudaMemsetAsync(dNodes, 0, static_cast<size_t>(n) * sizeof(u64), s));
   GPO_CK(cudaEventRecord(c->ev0, s));
   GPO_CK(launch_batched(a, cfg, c->sms, s));
+  c->launches += 1;
   GPO_CK(cudaEventRecord(c->ev1, s));
   GPO_CK(cudaMemcpyAsync(&pr->hs, c->dStats, sizeof(pr->hs), cudaMemcpyDeviceToHost, s));
   GPO_CK(cudaStreamSynchronize(s));
@@ -411,6 +416,7 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     // over-budget positions of this level
     GPO_CK(L.alloc(&L.idx, static_cast<size_t>(L.n)));
     GPO_CK(launch_collect_marked(L.score, L.n, L.idx, c->dCursor, s));
+    c->launches += 1;
     unsigned m = 0;
     GPO_CK(cudaMemcpyAsync(&m, c->dCursor, sizeof(m), cudaMemcpyDeviceToHost, s));
     GPO_CK(cudaStreamSynchronize(s));
@@ -429,6 +435,7 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     GPO_CK(cudaMemsetAsync(c->dCursor + 1, 0, sizeof(unsigned), s));
     GPO_CK(launch_expand(L.P, L.O, L.idx, L.m, cP, cO, C.parent, C.move, c->dCursor + 1,
                          static_cast<unsigned>(cap), s));
+    c->launches += 1;
     unsigned cn = 0;
     GPO_CK(cudaMemcpyAsync(&cn, c->dCursor + 1, sizeof(cn), cudaMemcpyDeviceToHost, s));
     GPO_CK(cudaStreamSynchronize(s));
@@ -445,6 +452,7 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     GPO_CK(cudaMemsetAsync(L.acc, 0, static_cast<size_t>(L.n) * sizeof(unsigned), s));
     GPO_CK(launch_combine(C.score, C.parent, C.move, C.nodes, C.n, L.acc, L.nodes, s));
     GPO_CK(launch_finalize(L.idx, L.m, L.acc, L.score, L.best, s));
+    c->launches += 2;
   }
   GPO_CK(cudaStreamSynchronize(s));
   if (stats) {
@@ -475,6 +483,7 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
     GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
     GPO_CK(cudaEventRecord(c->ev0, s));
     GPO_CK(launch_plain(dP, dO, n, depth, dScore, dNodes, c->dStats, s));
+    c->launches += 1;
     GPO_CK(cudaEventRecord(c->ev1, s));
     DeviceStats hs;
     GPO_CK(cudaMemcpyAsync(&hs, c->dStats, sizeof(hs), cudaMemcpyDeviceToHost, s));
@@ -505,11 +514,13 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
     unsigned count = 0;
     GPO_CK(ensure_second(c, static_cast<size_t>(n)) == GPO_OK ? cudaSuccess : cudaErrorMemoryAllocation);
     GPO_CK(launch_collect_marked(dScore, n, c->d2Idx, c->dCursor, s));
+    c->launches += 1;
     GPO_CK(cudaMemcpyAsync(&count, c->dCursor, sizeof(count), cudaMemcpyDeviceToHost, s));
     GPO_CK(cudaStreamSynchronize(s));
     if (count > 0) {
       const int m = static_cast<int>(count);
       GPO_CK(launch_gather(dP, dO, c->d2Idx, m, c->d2P, c->d2O, s));
+      c->launches += 1;
       PassConfig p2;
       p2.budget = 0;
       p2.mark = false;
@@ -520,6 +531,7 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
       if (rc == GPO_OK || rc == GPO_ERR_TIMEOUT) {
         GPO_CK(launch_scatter_scores(c->d2Score, c->d2Best, c->d2Nodes, c->d2Idx, m, dScore,
                                      dBest, dNodes, s));
+        c->launches += 1;
         GPO_CK(cudaStreamSynchronize(s));
       }
     }
@@ -570,6 +582,7 @@ int solve_batch_ex(const uint64_t* player, const uint64_t* opp, int n, int depth
   Context* c = nullptr;
   if ((rc = ensure_context(&c)) != GPO_OK) return rc;
   if ((rc = ensure_capacity(c, static_cast<size_t>(n))) != GPO_OK) return rc;
+  const unsigned long long launches0 = c->launches;
   cudaStream_t s = c->stream;
   GPO_CK(cudaMemcpyAsync(c->dP, player, n * sizeof(u64), cudaMemcpyHostToDevice, s));
   GPO_CK(cudaMemcpyAsync(c->dO, opp, n * sizeof(u64), cudaMemcpyHostToDevice, s));
@@ -581,9 +594,11 @@ int solve_batch_ex(const uint64_t* player, const uint64_t* opp, int n, int depth
   if (nodes)
     GPO_CK(cudaMemcpyAsync(nodes, c->dNodes, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
   GPO_CK(cudaStreamSynchronize(s));
-  if (stats)
+  if (stats) {
+    stats->launches = c->launches - launches0;
     stats->total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
   return rc;
 }
 
@@ -605,13 +620,16 @@ int solve_batch_device(const uint64_t* d_player, const uint64_t* d_opp, int n, i
   if ((rc = ensure_context(&c)) != GPO_OK) return rc;
   if ((rc = ensure_capacity(c, static_cast<size_t>(n))) != GPO_OK) return rc;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  const unsigned long long launches0 = c->launches;
   rc = run_solve(c, reinterpret_cast<const u64*>(d_player), reinterpret_cast<const u64*>(d_opp), n,
                  depth, reinterpret_cast<signed char*>(d_score),
                  reinterpret_cast<signed char*>(d_best_move),
                  reinterpret_cast<unsigned long long*>(d_nodes), opt, stats, s);
-  if (stats)
+  if (stats) {
+    stats->launches = c->launches - launches0;
     stats->total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
   return rc;
 }
 

@@ -85,8 +85,9 @@ cudaError_t batched_plan(int threads, int depth, int* smem_top);
 
 // Learned orderer (mlp.cu).
 bool mlp_loaded();
+// *launched receives the number of kernels it launched.
 int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
-                    u64* d_lists, cudaStream_t s);
+                    u64* d_lists, cudaStream_t s, unsigned* launched);
 
 // Positions whose score is -128 (over budget in a first pass), compacted:
 // idx[0..*count) = their indices, in order.

@@ -418,10 +418,12 @@ bool mlp_loaded() { return g_loaded; }
 // Root orders for the `count` positions d_idx[0..count) of d_player/d_opp:
 // d_lists[d_idx[i]] = packed list of the five best legal moves by logit.
 int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
-                    u64* d_lists, cudaStream_t s) {
+                    u64* d_lists, cudaStream_t s, unsigned* launched) {
+  *launched = 0;
   if (!g_loaded) return GPO_ERR_ARG;
   Net& t = g_infer;
   for (long off = 0; off < count; off += t.rows) {
+    *launched += 6;  // gather, three GEMMs, order, scatter
     gather_kernel<<<t.rows, 64, 0, s>>>(d_player, d_opp, d_idx, off, count, t.rows, t.X, t.legal,
                                          nullptr, nullptr);
     MLP_CK(cudaGetLastError());

@@ -81,6 +81,7 @@ typedef struct gpo_stats {
   uint64_t splits;        /* subtrees handed to other lanes */
   double kernel_ms;       /* device time of the search kernels (CUDA events) */
   double total_ms;        /* wall time of the call */
+  uint64_t launches;      /* kernels the call launched */
 } gpo_stats;
 
 /* Fills *opt with the defaults (all fields "auto"/0). */

@@ -43,6 +43,11 @@ def test_scores_match_reference(gpu, name, seed, count, lo, hi, depth, method):
     sc, _, _, st, _ = gpu.solve(p, o, depth, method=method, wait_limit_ms=60000)
     assert np.array_equal(sc.astype(int), scores)
     assert st.nodes > 0
+    # plain: the search kernel; batched: bucketing (3) + search, per pass
+    if method == PLAIN:
+        assert st.launches == 1
+    else:
+        assert st.launches >= 4
 
 
 @pytest.mark.parametrize("name,depth", [("c1_seed0_e10", 10), ("c3_seed2_mixed", 16),

@@ -89,3 +89,33 @@ def test_python_board_file_roundtrip(tmp_path):
     path = tmp_path / "b.txt"
     codec.write_board_file(str(path), p, o)
     assert path.read_text() == open(os.path.join(GOLDEN, "c1_seed0_e10.txt")).read()
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """The Python Options/Stats structures have the C structs' size and field
+    offsets (compiled from include/gpuothello2.h with the host compiler)."""
+    import gpuothello2_gb300 as g
+
+    structs = {"gpo_options": g.Options, "gpo_stats": g.Stats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gpuothello2.h"',
+             "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for field, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' %
+                         (cname, field, cname, field))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    c_layout = {}
+    for ln in out.splitlines():
+        cname, field, value = ln.split()
+        c_layout[(cname, field)] = int(value)
+    for cname, py in structs.items():
+        assert c_layout[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert c_layout[(cname, field)] == getattr(py, field).offset, (cname, field)
