@@ -62,6 +62,31 @@ def dist_env():
     return rank, world, local
 
 
+def slice_first(rank, n):
+    """First stream index of a rank's slice: rank r solves positions
+    [r*n, (r+1)*n) of the workload stream, so the ranks' slices are disjoint
+    and together form the first world*n positions (weak scaling)."""
+    return rank * n
+
+
+def max_over_ranks(seconds, world, device=None):
+    """The slowest rank's time (the job ends when every rank has finished);
+    a float64 all-reduce on the process group's backend."""
+    if world == 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, n, steps, seconds):
+    """Whole-job positions/s: every rank's positions over the slowest time."""
+    return world * n * steps / seconds
+
+
 class ClockSampler:
     """nvidia-smi sampling during the timed region (read-only queries)."""
 
@@ -202,8 +227,8 @@ def main():
     do = torch.empty(n, dtype=torch.int64, device=dev)
     ds = torch.empty(n, dtype=torch.int8, device=dev)
     stream = torch.cuda.current_stream(dev)
-    rc = L.gpo_generate_device(SEED, rank * n, n, LO, HI, dp.data_ptr(), do.data_ptr(),
-                               stream.cuda_stream)
+    rc = L.gpo_generate_device(SEED, slice_first(rank, n), n, LO, HI, dp.data_ptr(),
+                               do.data_ptr(), stream.cuda_stream)
     assert rc == 0, g.strerror(rc)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
@@ -276,14 +301,10 @@ def main():
     e2e_t = []
     step_ms, kern_ms, nodes = timed(g.METHOD_BATCHED, args.warmup, args.steps, sampler, e2e_t)
     batched_splits, batched_launches = list(timed.splits), int(sum(timed.launches))
-    total_s = sum(step_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * n * args.steps / total_s
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, world, dev)
+    value = job_value(world, n, args.steps, total_s)
     scores = ds.cpu().numpy()
-    e2e_value = world * n / e2e_t[0] if e2e_t else None
+    e2e_value = job_value(world, n, 1, max_over_ranks(e2e_t[0], world, dev)) if e2e_t else None
     if e2e_t:
         assert np.array_equal(hs.numpy(), scores), "host and device entry points disagree"
 
