@@ -201,6 +201,9 @@ def main():
     ap.add_argument("--n", type=int, default=N_POS)
     ap.add_argument("--split", type=int, default=0,
                     help="split_min_empties option (0 = library default, <0 = off)")
+    ap.add_argument("--tuned", action="store_true",
+                    help="autotune launch/search parameters on a 4,096-position sample of the "
+                         "batch first (untimed; cached per GPU, depth and empties range)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -231,6 +234,13 @@ def main():
                                do.data_ptr(), stream.cuda_stream)
     assert rc == 0, g.strerror(rc)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    tuned, tuned_src = {}, None
+    if args.tuned:
+        from gpuothello2_gb300 import autotune
+
+        params, tuned_src = autotune.tune_batch(dp.cpu().numpy().view(np.uint64),
+                                                do.cpu().numpy().view(np.uint64), DEPTH)
+        tuned = autotune.to_options(params)
 
     def barrier():
         if world > 1:
@@ -239,7 +249,8 @@ def main():
 
     def solve_device(method):
         st = g.Stats()
-        opt = g.options(method=method, split_min_empties=args.split)
+        opt = g.options(method=method, split_min_empties=args.split,
+                        **(tuned if method == g.METHOD_BATCHED else {}))
         rc = L.solve_batch_device(dp.data_ptr(), do.data_ptr(), n, DEPTH, ds.data_ptr(), None,
                                   None, ctypes.byref(opt), ctypes.byref(st), stream.cuda_stream)
         if rc != 0:
@@ -255,7 +266,7 @@ def main():
     def solve_host():
         """One step through the host-buffer entry point (pinned buffers):
         host->device copies, solve, device->host scores, wall clock."""
-        opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split)
+        opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split, **tuned)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         rc = L.solve_batch_ex(hp.data_ptr(), ho.data_ptr(), n, DEPTH, hs.data_ptr(), None, None,
@@ -342,7 +353,8 @@ def main():
         "data": "synthetic: seeded random playouts (xoshiro256**, seed 2), generated on device",
         "config": {"workload": WORKLOAD, "positions_per_gpu": n, "depth": DEPTH,
                    "l2": "flushed between steps (256 MiB write, untimed)",
-                   "method": "batched: empties-bucketed persistent queue"},
+                   "method": "batched: empties-bucketed persistent queue",
+                   "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None)},
         "e2e": {"value": e2e_value, "unit": "positions/s", "h2d_bytes_per_step": 16 * n,
                 "d2h_bytes_per_step": n,
                 "how": "last warm-up step through solve_batch_ex, pinned host buffers, wall clock"},

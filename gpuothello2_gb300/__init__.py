@@ -48,6 +48,8 @@ class Options(ctypes.Structure):
         ("wait_limit_ms", ctypes.c_int),
         ("table_bits", ctypes.c_int),
         ("table_min_empties", ctypes.c_int),
+        ("smem_frames", ctypes.c_int),
+        ("expand_budget", ctypes.c_uint64),
     ]
 
 

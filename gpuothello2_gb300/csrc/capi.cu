@@ -268,6 +268,11 @@ int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed 
   BatchedLaunch cfg;
   cfg.threads = o.threads_per_block > 0 ? o.threads_per_block : 128;
   GPO_CK(batched_plan(cfg.threads, depth, &a.smem_top));
+  // slots 2..smem_top live in shared memory: a cap only lowers the tier
+  if (o.smem_frames < 0)
+    a.smem_top = 1;
+  else if (o.smem_frames > 0 && a.smem_top > o.smem_frames + 1)
+    a.smem_top = o.smem_frames + 1;
   cfg.grid = 0;
   size_t smem = 0;
   GPO_CK(batched_grid(cfg.threads, a.smem_top, c->sms, &cfg.grid, &smem));
@@ -399,7 +404,7 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     Level& L = lv[k];
     const bool final_level = k == kExpandLevels - 1;
     PassConfig pc;
-    pc.budget = final_level ? 0 : kLevelBudget;
+    pc.budget = final_level ? 0 : (o.expand_budget > 0 ? o.expand_budget : kLevelBudget);
     pc.mark = !final_level;
     pc.split = false;
     pc.clear_table = k == 0;

@@ -63,13 +63,20 @@ typedef struct gpo_options {
   int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties; 0 = tuned */
   int learned_min_empties;    /* learned ordering at roots with >= this many empties; 0 = 14 */
   uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog) */
-  int split_min_empties;      /* hard positions (over 2^22 nodes in a first pass) are solved
-                                 again with their subtrees split across idle lanes, from
-                                 nodes with this many empties; 0 = 12, negative = never */
+  int split_min_empties;      /* hard positions: 0 = positions over expand_budget nodes are
+                                 replaced by their children, solved in further passes (up to
+                                 6 levels); > 0 = they are solved again with subtrees handed
+                                 to idle lanes from nodes with this many empties; negative =
+                                 one pass, no splitting */
   int wait_limit_ms;          /* deadline of one search launch (a watchdog on waits between
                                  lanes); 0 = 600000 */
   int table_bits;             /* transposition table of 2^table_bits 16-byte entries; 0 = 24 */
   int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 11 */
+  int smem_frames;            /* search frames kept in shared memory: 0 = as many as keep the
+                                 register-limited occupancy, > 0 = at most this many, negative
+                                 = none (every frame in the global frame array) */
+  uint64_t expand_budget;     /* split_min_empties == 0: per-position node budget of each
+                                 expansion level; 0 = 2^22 */
 } gpo_options;
 
 typedef struct gpo_stats {
