@@ -23,6 +23,11 @@ the timed region.
   cpu_baseline  the oracle's restatement of the reference tree on all host
          cores, on a bounded sample of the same stream
 
+Options: `--learned` trains the MLP move orderer first (untimed) and orders
+the roots of positions with >= 14 empties with it; `--tuned` autotunes the
+launch and search parameters on a sample of the batch first (untimed);
+`--plain` also times the plain kernel on the same batch.
+
 `--impl reference` times the reference algorithm on the host cores instead
 (the oracle port of the reference tree; the reference's own search only
 exists as GPU code), printing the same metric with "impl": "reference".
@@ -201,6 +206,12 @@ def main():
     ap.add_argument("--n", type=int, default=N_POS)
     ap.add_argument("--split", type=int, default=0,
                     help="split_min_empties option (0 = library default, <0 = off)")
+    ap.add_argument("--learned", action="store_true",
+                    help="train the MLP move orderer first (untimed: solver-labelled positions "
+                         "of seed 3 at 12-14 empties, GPU training kernels) and order the roots "
+                         "of positions with >= 14 empties with it")
+    ap.add_argument("--learned-train", type=int, default=1 << 20,
+                    help="training positions for --learned")
     ap.add_argument("--tuned", action="store_true",
                     help="autotune launch/search parameters on a 4,096-position sample of the "
                          "batch first (untimed; cached per GPU, depth and empties range)")
@@ -234,6 +245,17 @@ def main():
                                do.data_ptr(), stream.cuda_stream)
     assert rc == 0, g.strerror(rc)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    learned_info = None
+    if args.learned:
+        t0 = time.perf_counter()
+        tp, to = g.generate(3, args.learned_train, 12, 14)
+        _, labels, _, _, _ = g.solve(tp, to, 14, best=True)
+        w, hist = g.mlp_train(tp, to, labels, g.mlp_init(3), epochs=4, batch=2048, lr=1e-3,
+                              seed=1)
+        g.mlp_load(w)
+        learned_info = {"train_positions": args.learned_train, "epochs": 4,
+                        "loss_accuracy_per_epoch": hist,
+                        "setup_s": time.perf_counter() - t0, "min_empties": 14}
     tuned, tuned_src = {}, None
     if args.tuned:
         from gpuothello2_gb300 import autotune
@@ -250,6 +272,7 @@ def main():
     def solve_device(method):
         st = g.Stats()
         opt = g.options(method=method, split_min_empties=args.split,
+                        use_learned=1 if args.learned and method == g.METHOD_BATCHED else 0,
                         **(tuned if method == g.METHOD_BATCHED else {}))
         rc = L.solve_batch_device(dp.data_ptr(), do.data_ptr(), n, DEPTH, ds.data_ptr(), None,
                                   None, ctypes.byref(opt), ctypes.byref(st), stream.cuda_stream)
@@ -266,7 +289,8 @@ def main():
     def solve_host():
         """One step through the host-buffer entry point (pinned buffers):
         host->device copies, solve, device->host scores, wall clock."""
-        opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split, **tuned)
+        opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split,
+                        use_learned=1 if args.learned else 0, **tuned)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         rc = L.solve_batch_ex(hp.data_ptr(), ho.data_ptr(), n, DEPTH, hs.data_ptr(), None, None,
@@ -354,7 +378,8 @@ def main():
         "config": {"workload": WORKLOAD, "positions_per_gpu": n, "depth": DEPTH,
                    "l2": "flushed between steps (256 MiB write, untimed)",
                    "method": "batched: empties-bucketed persistent queue",
-                   "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None)},
+                   "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None),
+                   "learned": learned_info},
         "e2e": {"value": e2e_value, "unit": "positions/s", "h2d_bytes_per_step": 16 * n,
                 "d2h_bytes_per_step": n,
                 "how": "last warm-up step through solve_batch_ex, pinned host buffers, wall clock"},
