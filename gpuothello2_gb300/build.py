@@ -109,7 +109,7 @@ def build_oracle():
     src = os.path.join(ORACLE_DIR, "oracle.c")
     if _stale(ORACLE_LIB, [src, os.path.join(ORACLE_DIR, "oracle.h")]):
         _run(["gcc", "-O2", "-std=c11", "-Wall", "-shared", "-fPIC", "-pthread", src, "-o",
-              ORACLE_LIB])
+              ORACLE_LIB, "-lm"])
     return ORACLE_LIB
 
 

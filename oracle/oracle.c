@@ -5,6 +5,7 @@
  */
 #include "oracle.h"
 
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -489,6 +490,257 @@ int orc_solve_batch(const uint64_t* p, const uint64_t* o, int n, int depth, int 
   pthread_t tid[256];
   for (int t = 1; t < threads; ++t) pthread_create(&tid[t], NULL, batch_worker, &job);
   batch_worker(&job);
+  for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Pattern evaluator (eval.cu:12-141).  A feature is a square mask; its
+ * table has 3^k entries for k = popcount(mask), indexed by the base-3
+ * number whose digit j is 0 (empty), 1 (`me`) or 2 (`op`) on the mask's
+ * j-th lowest square (eval.cu:81-89, 107-113: base3[pext(me)] +
+ * 2 base3[pext(op)]).  The board is scored in all 8 symmetries: 4 rotations
+ * (rot90 = vertical flip after the A1-H8 transpose, eval.cu:102-104), each
+ * as is and transposed, features in file order, summed in float in exactly
+ * that order, plus the offset, clamped to [-64, 64] (eval.cu:129-141).
+ * Table values are read as doubles and stored as float (eval.cu:44-46). */
+struct orc_evaluator {
+  int n;
+  uint64_t feature[ORC_MAX_FEATURES];
+  float* value[ORC_MAX_FEATURES];
+  float offset;
+};
+
+static int pow3i(int k) {
+  int r = 1;
+  while (k-- > 0) r *= 3;
+  return r;
+}
+
+orc_evaluator* orc_eval_create(const uint64_t* features, int n, const double* values,
+                               double offset) {
+  if (n < 0 || n > ORC_MAX_FEATURES) return NULL;
+  orc_evaluator* ev = (orc_evaluator*)calloc(1, sizeof(orc_evaluator));
+  if (!ev) return NULL;
+  ev->n = n;
+  size_t off = 0;
+  for (int j = 0; j < n; ++j) {
+    ev->feature[j] = features[j];
+    const int len = pow3i(popc(features[j]));
+    ev->value[j] = (float*)malloc(sizeof(float) * (size_t)len);
+    for (int i = 0; i < len; ++i) ev->value[j][i] = (float)values[off + (size_t)i];
+    off += (size_t)len;
+  }
+  ev->offset = (float)offset;
+  return ev;
+}
+
+void orc_eval_free(orc_evaluator* ev) {
+  if (!ev) return;
+  for (int j = 0; j < ev->n; ++j) free(ev->value[j]);
+  free(ev);
+}
+
+/* base-3 index of the mask's squares: digit 1 for `me`, 2 for `op` */
+static int feature_index(uint64_t me, uint64_t op, uint64_t mask) {
+  int idx = 0, w = 1;
+  while (mask) {
+    const uint64_t b = mask & (0 - mask);
+    mask ^= b;
+    if (me & b) idx += w;
+    if (op & b) idx += 2 * w;
+    w *= 3;
+  }
+  return idx;
+}
+
+/* transpose about the A1-H8 diagonal: square (r, c) -> (c, r) */
+static uint64_t transpose(uint64_t x) {
+  uint64_t y = 0;
+  for (int sq = 0; sq < 64; ++sq)
+    if ((x >> sq) & 1) y |= 1ULL << ((sq % 8) * 8 + sq / 8);
+  return y;
+}
+
+/* vertical flip: row r -> row 7 - r */
+static uint64_t flip_rows(uint64_t x) {
+  uint64_t y = 0;
+  for (int r = 0; r < 8; ++r) y |= ((x >> (8 * r)) & 0xFF) << (8 * (7 - r));
+  return y;
+}
+
+float orc_eval(const orc_evaluator* ev, uint64_t me, uint64_t op) {
+  float score = 0.0f;
+  for (int i = 0; i < 4; ++i) {
+    const uint64_t tme = transpose(me), top = transpose(op);
+    for (int j = 0; j < ev->n; ++j) {
+      score += ev->value[j][feature_index(me, op, ev->feature[j])];
+      score += ev->value[j][feature_index(tme, top, ev->feature[j])];
+    }
+    me = flip_rows(tme);
+    op = flip_rows(top);
+  }
+  const float s = score + ev->offset;
+  return s > 64.0f ? 64.0f : (s < -64.0f ? -64.0f : s);
+}
+
+/* ------------------------------------------------------------------ */
+/* Think mode (thinker.cu:12-376): depth-limited fail-soft negamax.  The
+ * first depth-3 plies are "upper" nodes (thinker.cu:14-107): legal moves
+ * ordered by the opponent's move count after the move, stably, from the
+ * corners-first scan; result starts at -65 and a commit that raises it
+ * records the move (thinker.cu:97-103).  The last 3 plies are the
+ * reference's lower nodes (node.cuh:56-74, thinker.cu:226-262), as in the
+ * solve path.  A move at the last lower ply reaches a leaf scored
+ * round(eval(leaf)) (thinker.cu:324-326, 200-204); a game that ends before
+ * that depth is scored exactly.  Passes take no ply.  The root's best move
+ * is 64 (pass) when the root passed (thinker.cu:167-170).  Steps count the
+ * reference's loop iterations (thinker.cu:321-335); nodes count the root,
+ * every pushed child, pass frame and leaf. */
+typedef struct {
+  const orc_evaluator* ev;
+  int upper_size, depth;
+  uint64_t steps, nodes;
+} think_ctx;
+
+static int think_lower(think_ctx* cx, uint64_t p, uint64_t o, int alpha, int beta, int level) {
+  cx->nodes++;
+  int passed = 0;
+  for (;;) {
+    int result = -32767, found = 0;
+    uint64_t unchecked = ~(p | o);
+    while (unchecked) {
+      if (alpha >= beta) {
+        cx->steps++;
+        return passed ? -result : result;
+      }
+      cx->steps++;
+      const uint64_t bit = scan_next(&unchecked);
+      const uint64_t f = orc_flip(p, o, ctz(bit));
+      if (f) {
+        found = 1;
+        int v;
+        if (level == cx->depth - 1) {
+          cx->steps++; /* the leaf's own step */
+          cx->nodes++;
+          v = -(int)roundf(orc_eval(cx->ev, o ^ f, p ^ f ^ bit));
+        } else {
+          v = -think_lower(cx, o ^ f, p ^ f ^ bit, -beta, -alpha, level + 1);
+        }
+        if (v > result) result = v;
+        if (result > alpha) alpha = result;
+      }
+    }
+    if (found) {
+      cx->steps++;
+      return passed ? -result : result;
+    }
+    cx->steps++;
+    if (passed) return -orc_final_score(p, o);
+    cx->nodes++; /* the pass frame */
+    passed = 1;
+    const uint64_t t = p;
+    p = o;
+    o = t;
+    const int a = alpha;
+    alpha = -beta;
+    beta = -a;
+  }
+}
+
+static int think_upper(think_ctx* cx, uint64_t p, uint64_t o, int alpha, int beta, int ply,
+                       int* best) {
+  cx->nodes++;
+  move_list ml;
+  int passed = 0;
+  upper_moves(p, o, &ml);
+  if (ml.n == 0) {
+    cx->steps++; /* pass_upper */
+    cx->nodes++;
+    passed = 1;
+    const uint64_t t = p;
+    p = o;
+    o = t;
+    const int a = alpha;
+    alpha = -beta;
+    beta = -a;
+    upper_moves(p, o, &ml);
+    if (ml.n == 0) {
+      cx->steps++;
+      *best = 64;
+      return -orc_final_score(p, o);
+    }
+  }
+  int result = -65, bm = 65, child_best = 65;
+  for (int i = 0; i < ml.n; ++i) {
+    if (alpha >= beta) break;
+    cx->steps++;
+    const uint64_t bit = 1ULL << ml.sq[i];
+    const uint64_t f = orc_flip(p, o, ml.sq[i]);
+    int v;
+    if (ply + 1 < cx->upper_size)
+      v = -think_upper(cx, o ^ f, p ^ f ^ bit, -beta, -alpha, ply + 1, &child_best);
+    else
+      v = -think_lower(cx, o ^ f, p ^ f ^ bit, -beta, -alpha, ply + 1);
+    if (v > result) {
+      result = v;
+      bm = ml.sq[i];
+      if (result > alpha) alpha = result;
+    }
+  }
+  cx->steps++;
+  *best = passed ? 64 : bm;
+  return passed ? -result : result;
+}
+
+int orc_think(const orc_evaluator* ev, uint64_t p, uint64_t o, int depth, int* best,
+              uint64_t* steps, uint64_t* nodes) {
+  ensure_tables();
+  think_ctx cx = {ev, depth - 3, depth, 0, 0};
+  int b = 65;
+  const int v = think_upper(&cx, p, o, -64, 64, 0, &b);
+  if (best) *best = b;
+  if (steps) *steps = cx.steps;
+  if (nodes) *nodes = cx.nodes;
+  return v;
+}
+
+typedef struct {
+  const orc_evaluator* ev;
+  const uint64_t *p, *o;
+  int n, depth;
+  int8_t *score, *best;
+  uint64_t *steps, *nodes;
+  int next;
+} think_job;
+
+static void* think_worker(void* arg) {
+  think_job* job = (think_job*)arg;
+  for (;;) {
+    const int i = __atomic_fetch_add(&job->next, 1, __ATOMIC_RELAXED);
+    if (i >= job->n) break;
+    uint64_t st = 0, nd = 0;
+    int b = 65;
+    const int v = orc_think(job->ev, job->p[i], job->o[i], job->depth, &b, &st, &nd);
+    job->score[i] = (int8_t)v;
+    if (job->best) job->best[i] = (int8_t)b;
+    if (job->steps) job->steps[i] = st;
+    if (job->nodes) job->nodes[i] = nd;
+  }
+  return NULL;
+}
+
+int orc_think_batch(const orc_evaluator* ev, const uint64_t* p, const uint64_t* o, int n,
+                    int depth, int threads, int8_t* score, int8_t* best, uint64_t* steps,
+                    uint64_t* nodes) {
+  ensure_tables();
+  if (depth < 4) return -1;
+  if (threads <= 0) threads = orc_num_cores();
+  if (threads > 256) threads = 256;
+  think_job job = {ev, p, o, n, depth, score, best, steps, nodes, 0};
+  pthread_t tid[256];
+  for (int t = 1; t < threads; ++t) pthread_create(&tid[t], NULL, think_worker, &job);
+  think_worker(&job);
   for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
   return 0;
 }

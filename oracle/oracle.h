@@ -12,6 +12,8 @@
  *     negamax with pass handling (solver.cu:75-283, node.cuh:5-74)
  *   - the base81 board codec (test.cpp:7-19 encoder, to_board.cpp:15-39
  *     decoder semantics)
+ *   - the pattern evaluator and the depth-limited think-mode search
+ *     (eval.cu:12-141, thinker.cu:12-376)
  * plus an independent fast alpha-beta solver (different move ordering, so
  * a second opinion on every score) and the seeded random-playout position
  * generator that defines the benchmark inputs.
@@ -63,6 +65,27 @@ int orc_solve_fast(uint64_t p, uint64_t o, uint64_t* nodes, int* best);
 int orc_solve_batch(const uint64_t* p, const uint64_t* o, int n, int depth, int mode,
                     int threads, int8_t* score, uint64_t* steps, uint64_t* nodes, int8_t* best);
 int orc_num_cores(void);
+
+/* ---- pattern evaluator and think mode (eval.cu, thinker.cu) ---- */
+#define ORC_MAX_FEATURES 32
+typedef struct orc_evaluator orc_evaluator;
+/* features[n] square masks; values = the tables of all features in order
+ * (3^popcount(mask) doubles each, as in the reference's value file) and
+ * the offset.  Returns NULL on bad arguments or allocation failure. */
+orc_evaluator* orc_eval_create(const uint64_t* features, int n, const double* values,
+                               double offset);
+void orc_eval_free(orc_evaluator* ev);
+/* Evaluator::eval (eval.cu:129-141): me = side to move. */
+float orc_eval(const orc_evaluator* ev, uint64_t me, uint64_t op);
+/* think_kernel's search of one position to `depth` plies (>= 4): returns
+ * the value; *best = the root's best move (64 = pass); *steps = the
+ * reference's loop-step count; *nodes = root, children, pass frames and
+ * leaves. */
+int orc_think(const orc_evaluator* ev, uint64_t p, uint64_t o, int depth, int* best,
+              uint64_t* steps, uint64_t* nodes);
+int orc_think_batch(const orc_evaluator* ev, const uint64_t* p, const uint64_t* o, int n,
+                    int depth, int threads, int8_t* score, int8_t* best, uint64_t* steps,
+                    uint64_t* nodes);
 
 #ifdef __cplusplus
 }

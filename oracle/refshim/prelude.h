@@ -19,6 +19,11 @@
  *   - the CUDA runtime calls used by the host halves of those files
  *     (cudaMalloc*, cudaMemcpy, cudaMemset, streams) are backed by malloc.
  *
+ * The evaluator and think-mode search (eval.cu, thinker.cu) are compiled
+ * the same way; eval.cu with __CUDA_ARCH__ defined, so that its device
+ * branch (the software bit-extract loop and __ldg loads, eval.cu:67-79,
+ * 115-139) is the code emulated, as on the GPU.
+ *
  * The device intrinsics __popcll/__clzll are only reached through
  * `#ifdef __CUDA_ARCH__` branches or solver.cu:85; they are restated with
  * the GCC builtins and clz(0) defined as 64.
@@ -27,6 +32,7 @@
 #include <algorithm>
 #include <cassert>
 #include <climits>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
@@ -41,6 +47,17 @@
 
 using std::max;
 using std::min;
+/* CUDA's math headers also overload min/max for mixed double/float
+ * arguments, returning double; the evaluator's clamp (eval.cu:140) uses
+ * them.  Same-type calls still resolve to std::min/std::max. */
+inline double max(double a, double b) { return a > b ? a : b; }
+inline double min(double a, double b) { return a < b ? a : b; }
+
+/* Read-only-cache load (eval.cu:119-136): a plain load on one CPU thread. */
+template <class T>
+inline T __ldg(const T* p) {
+  return *p;
+}
 
 struct refshim_dim3 {
   unsigned int x, y, z;

@@ -22,6 +22,18 @@ reference's ascending (player, opponent) order, from `refsolve --per-board`):
   codec_vectors.txt          2,000 random disjoint boards encoded by the
                              reference's fromBoard ("<p hex> <o hex> <str>")
 
+Think mode (reference's eval.cu + thinker.cu, `refthink --per-board`), with
+the pattern set and synthetic weights of think_data.py; *.ref lines are
+"<base81> <score> <best move> <loop steps>":
+
+  think_seed6_e24_34_d6      240 positions, seed 6, 24..34 empties, depth 6
+  think_seed7_e6_12_d4       400 positions, seed 7, 6..12 empties, depth 4
+  think_seed8_e20_28_d8      24 positions, seed 8, 20..28 empties, depth 8
+  think_edge_d5              think_data.edge_boards(), depth 5
+  eval_vectors.txt           Evaluator::eval of 2,000 positions of seed 9
+                             (4..60 empties) and the edge boards,
+                             "<p hex> <o hex> <float bits hex>"
+
 Usage: python tests/golden/make_golden.py [--only NAME ...]
 """
 import argparse
@@ -39,6 +51,13 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 README9 = None  # read from the reference README at run time (lines 11-19)
+
+THINK_FIXTURES = {
+    # name: (seed, count, min_empties, max_empties, think depth)
+    "think_seed6_e24_34_d6": (6, 240, 24, 34, 6),
+    "think_seed7_e6_12_d4": (7, 400, 6, 12, 4),
+    "think_seed8_e20_28_d8": (8, 24, 20, 28, 8),
+}
 
 FIXTURES = {
     # name: (seed, count, min_empties, max_empties, depth)
@@ -80,17 +99,18 @@ def generate_lines(lib, seed, count, lo, hi):
     return out
 
 
-def run_reference(refsolve, lines, depth, jobs):
+def run_reference(refsolve, lines, depth, jobs, prefix=()):
     """Runs the reference per board on `jobs` processes; returns its lines
-    re-sorted into the reference's (player, opponent) order."""
+    re-sorted into the reference's (player, opponent) order.  `prefix` goes
+    before the board-file arguments (refthink's feature and value files)."""
     chunks = [lines[i::jobs] for i in range(jobs) if lines[i::jobs]]
     with tempfile.TemporaryDirectory() as td:
         def one(k):
             inp = os.path.join(td, "in%d.txt" % k)
             out = os.path.join(td, "out%d.txt" % k)
             write_boards(inp, chunks[k])
-            subprocess.run([refsolve, inp, out, str(depth), "--per-board"], check=True,
-                           stderr=subprocess.DEVNULL)
+            subprocess.run([refsolve, *prefix, inp, out, str(depth), "--per-board"],
+                           check=True, stderr=subprocess.DEVNULL)
             return open(out).read().splitlines()
 
         with ThreadPoolExecutor(jobs) as ex:
@@ -129,12 +149,53 @@ def main():
         with open(os.path.join(HERE, "readme9.ref"), "w") as f:
             f.write("\n".join(ref) + "\n")
         print("readme9", len(ref))
+    if not want or want & (set(THINK_FIXTURES) | {"think_edge_d5", "eval_vectors"}):
+        make_think(lib, want, args.jobs)
     if not want or "codec" in want:
         out = subprocess.run([refsolve, "--codec", "2000", "20261203"], check=True,
                              capture_output=True, text=True).stdout
         with open(os.path.join(HERE, "codec_vectors.txt"), "w") as f:
             f.write(out)
         print("codec_vectors", len(out.splitlines()))
+
+
+def make_think(lib, want, jobs):
+    from tests.golden import think_data as T
+
+    refthink = os.path.join(ROOT, "oracle", "_ref", "refthink")
+    with tempfile.TemporaryDirectory() as td:
+        feat, val = os.path.join(td, "features.txt"), os.path.join(td, "values.bin")
+        T.write_features(feat)
+        T.write_values(val)
+        buf = ctypes.create_string_buffer(17)
+
+        def encode(pairs):
+            out = []
+            for p, o in pairs:
+                lib.orc_encode(int(p), int(o), buf)
+                out.append(buf.value.decode())
+            return out
+
+        cases = {name: (generate_lines(lib, seed, count, lo, hi), depth)
+                 for name, (seed, count, lo, hi, depth) in THINK_FIXTURES.items()}
+        cases["think_edge_d5"] = (encode(T.edge_boards()), 5)
+        for name, (lines, depth) in cases.items():
+            if want and name not in want:
+                continue
+            write_boards(os.path.join(HERE, name + ".txt"), lines)
+            ref = run_reference(refthink, lines, depth, jobs, prefix=(feat, val))
+            with open(os.path.join(HERE, name + ".ref"), "w") as f:
+                f.write("\n".join(ref) + "\n")
+            print(name, len(lines), "boards,", len(ref), "unique")
+        if not want or "eval_vectors" in want:
+            lines = generate_lines(lib, 9, 2000, 4, 60) + encode(T.edge_boards())
+            inp = os.path.join(td, "eval_in.txt")
+            write_boards(inp, lines)
+            out = subprocess.run([refthink, "--eval", feat, val, inp], check=True,
+                                 capture_output=True, text=True).stdout
+            with open(os.path.join(HERE, "eval_vectors.txt"), "w") as f:
+                f.write(out)
+            print("eval_vectors", len(out.splitlines()))
 
 
 if __name__ == "__main__":
