@@ -32,6 +32,7 @@ EXPORTED_SYMBOLS = (
     "gpo_generate", "gpo_generate_device", "solve_shutdown", "gpo_strerror",
     "gpo_device_info", "solve_batch_device_noalloc", "gpo_mlp_param_count", "gpo_mlp_init",
     "gpo_mlp_forward", "gpo_mlp_gradients", "gpo_mlp_train", "gpo_mlp_load",
+    "gpo_eval_load", "gpo_eval_load_files", "gpo_evaluate", "think_batch",
 )
 
 
@@ -109,6 +110,10 @@ def lib():
         L.gpo_mlp_gradients.argtypes = [vp, vp, vp, vp, i, vp, ctypes.POINTER(f32)]
         L.gpo_mlp_train.argtypes = [vp, vp, vp, i, i, i, f32, u64, vp, vp]
         L.gpo_mlp_load.argtypes = [vp]
+        L.gpo_eval_load.argtypes = [vp, i, vp, ctypes.c_double]
+        L.gpo_eval_load_files.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        L.gpo_evaluate.argtypes = [vp, vp, i, vp]
+        L.think_batch.argtypes = [vp, vp, i, i, vp, vp, vp, ctypes.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -242,3 +247,45 @@ def mlp_load(w):
         rc = lib().gpo_mlp_load(w.ctypes.data)
     if rc != GPO_OK:
         raise SolverError(rc, "gpo_mlp_load")
+
+
+def eval_load(features, values, offset):
+    """Loads the think-mode pattern evaluator: square masks, every feature's
+    table (3^k values) in order, and the offset."""
+    f = np.ascontiguousarray(features, np.uint64)
+    v = np.ascontiguousarray(values, np.float64)
+    rc = lib().gpo_eval_load(f.ctypes.data, len(f), v.ctypes.data, float(offset))
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_eval_load")
+
+
+def eval_load_files(features_path, values_path):
+    """Loads the evaluator from the reference's feature and value files."""
+    rc = lib().gpo_eval_load_files(os.fsencode(features_path), os.fsencode(values_path))
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_eval_load_files")
+
+
+def evaluate(player, opp):
+    p, o = _u64(player), _u64(opp)
+    out = np.zeros(len(p), np.float32)
+    rc = lib().gpo_evaluate(p.ctypes.data, o.ctypes.data, len(p), out.ctypes.data)
+    if rc != GPO_OK:
+        raise SolverError(rc, "gpo_evaluate")
+    return out
+
+
+def think(player, opp, depth, check=True):
+    """Think mode through think_batch.  Returns (score, best move, nodes,
+    stats, status)."""
+    p, o = _u64(player), _u64(opp)
+    n = len(p)
+    score = np.zeros(n, np.int8)
+    best = np.zeros(n, np.int8)
+    nodes = np.zeros(n, np.uint64)
+    st = Stats()
+    rc = lib().think_batch(p.ctypes.data, o.ctypes.data, n, depth, score.ctypes.data,
+                           best.ctypes.data, nodes.ctypes.data, ctypes.byref(st))
+    if check and rc != GPO_OK:
+        raise SolverError(rc, "think_batch")
+    return score, best, nodes, st, rc

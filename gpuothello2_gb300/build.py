@@ -4,8 +4,10 @@
   bin/solver             C++ CLI `solver INPUT OUTPUT DEPTH` over the C ABI
   bin/gen_boards         C++ board-file generator over the C ABI
   oracle/lib/liboracle.so  CPU oracle (test infrastructure, not the product)
-  oracle/_ref/refsolve   the reference's own search built for the CPU, only
-                         where the reference sources are present (x86-64)
+  oracle/lib/libthink_host.so  csrc/think.cuh compiled for the CPU (tests only)
+  oracle/_ref/refsolve, refthink  the reference's own search and think mode
+                         built for the CPU, only where the reference sources
+                         are present (x86-64)
 
 Translation units are compiled in parallel; a unit is rebuilt only when a
 source it depends on (same directory headers included) is newer.
@@ -29,6 +31,8 @@ SOLVER_BIN = os.path.join(BIN_DIR, "solver")
 GEN_BIN = os.path.join(BIN_DIR, "gen_boards")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "lib", "liboracle.so")
+# host build of csrc/think.cuh for the CPU tests (test infrastructure)
+THINK_HOST_LIB = os.path.join(ORACLE_DIR, "lib", "libthink_host.so")
 REF_BIN = os.path.join(ORACLE_DIR, "_ref", "refsolve")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -36,7 +40,7 @@ NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 
-CU_SOURCES = ["plain.cu", "batched.cu", "prep.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
+CU_SOURCES = ["plain.cu", "batched.cu", "prep.cu", "capi.cu", "noalloc.cu", "mlp.cu", "think.cu"]
 INTPEAK_LIB = os.path.join(LIB_DIR, "libgpo_intpeak.so")
 
 
@@ -113,6 +117,19 @@ def build_oracle():
     return ORACLE_LIB
 
 
+def build_think_host():
+    """tests/think_host.cpp: the think-mode search and evaluator header
+    compiled for the CPU, for tests only."""
+    os.makedirs(os.path.dirname(THINK_HOST_LIB), exist_ok=True)
+    src = os.path.join(ROOT, "tests", "think_host.cpp")
+    deps = [src, os.path.join(CSRC, "think.cuh"), os.path.join(CSRC, "evalfile.h"),
+            os.path.join(ROOT, "include", "gpuothello2.h")]
+    if _stale(THINK_HOST_LIB, deps):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", "-shared", "-fPIC", src, "-o",
+              THINK_HOST_LIB])
+    return THINK_HOST_LIB
+
+
 def build_reference():
     """The reference's search compiled for the CPU (oracle/ref_build.sh);
     a no-op where the reference sources or an x86-64 host are absent."""
@@ -122,12 +139,14 @@ def build_reference():
 
 
 def build_all(verbose=False):
-    with ThreadPoolExecutor(3) as ex:
+    with ThreadPoolExecutor(4) as ex:
         f_lib = ex.submit(build_library, verbose)
         f_orc = ex.submit(build_oracle)
+        f_th = ex.submit(build_think_host)
         f_ref = ex.submit(build_reference)
         f_lib.result()
         f_orc.result()
+        f_th.result()
         f_ref.result()
     build_host()
 

@@ -109,6 +109,34 @@ bool write_results(const std::string& path, const std::vector<Board>& boards,
   return true;
 }
 
+std::string move_string(int move) {
+  if (move == 64) return "ps";
+  std::string s(1, static_cast<char>('A' + move % 8));
+  s += static_cast<char>('1' + move / 8);
+  return s;
+}
+
+bool write_think_results(const std::string& path, const std::vector<Board>& boards,
+                         const std::vector<int8_t>& score, const std::vector<int8_t>& best,
+                         std::string& err) {
+  std::FILE* fp = std::fopen(path.c_str(), "w");
+  if (!fp) {
+    err = "cannot open " + path + " for writing";
+    return false;
+  }
+  char buf[17];
+  for (size_t i = 0; i < boards.size(); ++i) {
+    encode(boards[i].p, boards[i].o, buf);
+    std::fprintf(fp, "%s %d %s\n", buf, static_cast<int>(score[i]),
+                 move_string(best[i]).c_str());
+  }
+  if (std::fclose(fp) != 0) {
+    err = "write failed: " + path;
+    return false;
+  }
+  return true;
+}
+
 bool write_boards(const std::string& path, const std::vector<Board>& boards, std::string& err) {
   std::FILE* fp = std::fopen(path.c_str(), "w");
   if (!fp) {

@@ -32,6 +32,13 @@ bool load_boards(const std::string& path, std::vector<Board>& out, std::string& 
 bool write_results(const std::string& path, const std::vector<Board>& boards,
                    const std::vector<int8_t>& score, std::string& err);
 
+// Think mode: "<base81> <score> <move>\n" per board (main.cu:114-117), the
+// move as column letter + row digit, "ps" for a pass (main.cu:31-39).
+bool write_think_results(const std::string& path, const std::vector<Board>& boards,
+                         const std::vector<int8_t>& score, const std::vector<int8_t>& best,
+                         std::string& err);
+std::string move_string(int move);
+
 bool write_boards(const std::string& path, const std::vector<Board>& boards, std::string& err);
 
 }  // namespace gpo_host

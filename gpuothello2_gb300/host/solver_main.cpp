@@ -1,16 +1,19 @@
-// `solver INPUT OUTPUT DEPTH` -- the reference CLI's solve mode
-// (main.cu:123-185) over the C ABI.
+// `solver INPUT OUTPUT DEPTH [THINK_DEPTH]` -- the reference CLI
+// (main.cu:69-185) over the C ABI.
 //
-// Same arguments, input format, sort + dedup, output lines and stderr lines
-// as the reference; additionally prints throughput.  Differences: errors
-// (unreadable file, bad board line, a position with more empties than
-// DEPTH, CUDA failures) end with a message and a nonzero exit instead of
-// undefined behaviour, and the 5-argument think mode (main.cu:69-121) is
-// rejected because its pattern weights (value/value52, main.cu:75) are not
-// part of the reference.
+// Solve mode (3 arguments, main.cu:123-173) and think mode (4 arguments,
+// main.cu:69-121): same arguments, input format, sort + dedup, output lines
+// and stderr lines as the reference; additionally prints throughput.  Think
+// mode reads the pattern evaluator from "subboard.txt" and "value/value52"
+// in the working directory, as the reference does (main.cu:74); the
+// environment variables GPO_FEATURES_FILE and GPO_VALUES_FILE override the
+// two paths.  DEPTH is read but unused in think mode, as in the reference.
+// Differences: errors (unreadable file, bad board line, a position with more
+// empties than DEPTH, a missing evaluator file, CUDA failures) end with a
+// message and a nonzero exit instead of undefined behaviour.
 //
 // Environment: GPO_METHOD=plain selects the plain thread-per-board kernel
-// (default: batched).
+// for solve mode (default: batched).
 #include <chrono>
 #include <cinttypes>
 #include <cstdio>
@@ -22,17 +25,76 @@
 #include "boardfile.h"
 #include "gpuothello2.h"
 
+namespace {
+
+long parse_int(const char* s) {
+  char* end = nullptr;
+  const long v = std::strtol(s, &end, 10);
+  return (end && *end == '\0' && end != s) ? v : -1;
+}
+
+int think_main(char** argv) {
+  const long depth = parse_int(argv[4]);
+  if (depth < 4 || depth > 24) {
+    std::fprintf(stderr, "THINK_DEPTH must be an integer in [4, 24]\n");
+    return 1;
+  }
+  std::vector<gpo_host::Board> boards;
+  std::string err;
+  if (!gpo_host::load_boards(argv[1], boards, err)) {
+    std::fprintf(stderr, "%s\n", err.c_str());
+    return EXIT_FAILURE;
+  }
+  const char* fpath = std::getenv("GPO_FEATURES_FILE");
+  const char* vpath = std::getenv("GPO_VALUES_FILE");
+  if (!fpath) fpath = "subboard.txt";
+  if (!vpath) vpath = "value/value52";
+  const int lrc = gpo_eval_load_files(fpath, vpath);
+  if (lrc != GPO_OK) {
+    std::fprintf(stderr, "cannot load the pattern evaluator from %s and %s: %s\n", fpath, vpath,
+                 gpo_strerror(lrc));
+    return EXIT_FAILURE;
+  }
+  const size_t n = boards.size();
+  std::fprintf(stderr, "n = %zu\n", n);
+  std::vector<uint64_t> p(n), o(n);
+  for (size_t i = 0; i < n; ++i) {
+    p[i] = boards[i].p;
+    o[i] = boards[i].o;
+  }
+  std::vector<int8_t> score(n, 0), best(n, 0);
+  gpo_stats st;
+  std::memset(&st, 0, sizeof(st));
+  const auto t0 = std::chrono::steady_clock::now();
+  const int rc = think_batch(p.data(), o.data(), static_cast<int>(n), static_cast<int>(depth),
+                             score.data(), best.data(), nullptr, &st);
+  const auto t1 = std::chrono::steady_clock::now();
+  const long ms = static_cast<long>(
+      std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count());
+  std::fprintf(stderr,
+               "%s (%s), elapsed: %ldms, table update count: 0, table hit: 0, table find: 0\n",
+               rc == GPO_OK ? "cudaSuccess" : "error", rc == GPO_OK ? "no error" : gpo_strerror(rc),
+               ms);
+  if (rc != GPO_OK) return EXIT_FAILURE;
+  const double sec = std::chrono::duration<double>(t1 - t0).count();
+  std::fprintf(stderr, "positions/s: %.0f, nodes/s: %.4g, kernel: %.3fms\n",
+               sec > 0 ? n / sec : 0.0, sec > 0 ? st.nodes / sec : 0.0, st.kernel_ms);
+  if (!gpo_host::write_think_results(argv[2], boards, score, best, err)) {
+    std::fprintf(stderr, "%s\n", err.c_str());
+    return EXIT_FAILURE;
+  }
+  std::fprintf(stderr, "total nodes: %" PRIu64 "\n", st.nodes);
+  return 0;
+}
+
+}  // namespace
+
 int main(int argc, char** argv) {
   if (argc < 4) {
     std::fprintf(stderr, "usage: %s INPUT OUTPUT DEPTH [THINK_DEPTH]\n", argv[0]);
     return 1;
   }
-  if (argc >= 5) {
-    std::fprintf(stderr,
-                 "think mode (THINK_DEPTH) is not supported: it needs the pattern weights "
-                 "value/value52, which the reference does not ship\n");
-    return 2;
-  }
+  if (argc == 5) return think_main(argv);
   char* end = nullptr;
   const long depth = std::strtol(argv[3], &end, 10);
   if (!end || *end != '\0' || depth < 1 || depth > 32) {

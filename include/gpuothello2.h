@@ -178,6 +178,38 @@ int gpo_mlp_train(const uint64_t* player, const uint64_t* opp, const int8_t* bes
                   int epochs, int batch, float lr, uint64_t seed, float* weights, float* history);
 int gpo_mlp_load(const float* weights);
 
+/*
+ * Think mode: depth-limited search with a pattern evaluator, the reference's
+ * `solver INPUT OUTPUT DEPTH THINK_DEPTH` path (main.cu:69-121).
+ *
+ * gpo_eval_load replaces Evaluator's constructor (eval.cu:12-60):
+ * features[n_features] are square masks (at most 32 features of at most 12
+ * squares each); values holds every feature's table in order (3^k doubles
+ * for a k-square feature, indexed by the base-3 number whose digit j is 0
+ * empty, 1 side to move, 2 other side on the mask's j-th lowest square),
+ * stored as float like the reference; offset is added to the sum.
+ * gpo_eval_load_files reads the same from the reference's feature file
+ * (count, then 8 rows of 8 binary digits per feature) and value file
+ * (binary doubles, then the offset); GPO_ERR_IO if a file is missing or
+ * short, GPO_ERR_ARG if malformed.
+ */
+int gpo_eval_load(const uint64_t* features, int n_features, const double* values, double offset);
+int gpo_eval_load_files(const char* features_path, const char* values_path);
+/* Evaluator::eval (eval.cu:129-141) of n positions: the sum over the 8
+ * board symmetries and all features, plus the offset, clamped to [-64, 64].
+ * GPO_ERR_ARG if no evaluator is loaded. */
+int gpo_evaluate(const uint64_t* player, const uint64_t* opp, int n, float* value);
+/* Replaces BatchedThinkTask + think_kernel (thinker.cuh:9-29,
+ * thinker.cu:12-389): searches each position `depth` plies (4..24; passes
+ * take none) and scores the positions reached with round(eval); games that
+ * end earlier are scored exactly.  score[i] = the value for the side to
+ * move; best_move[i] (optional) = its move, 64 = pass; nodes[i] (optional)
+ * = positions visited (root, children, pass frames, leaves).  Any number of
+ * empty squares.  GPO_ERR_ARG if no evaluator is loaded, GPO_ERR_DEPTH for
+ * a depth outside 4..24, GPO_ERR_BOARD for overlapping bitboards. */
+int think_batch(const uint64_t* player, const uint64_t* opp, int n, int depth, int8_t* score,
+                int8_t* best_move, uint64_t* nodes, gpo_stats* stats);
+
 /* Releases the library context (device buffers, table, stream). */
 void solve_shutdown(void);
 

@@ -60,9 +60,18 @@ def test_cli_usage_and_think_mode(built):
     r = run_cli([])
     assert r.returncode == 1 and "usage:" in r.stderr
     r = run_cli(["a", "b", "10", "3"])
-    assert r.returncode == 2 and "think mode" in r.stderr
+    assert r.returncode == 1 and "THINK_DEPTH" in r.stderr
     r = run_cli(["a", "b", "x"])
     assert r.returncode == 1
+
+
+def test_cli_think_mode_needs_the_evaluator_files(built, tmp_path):
+    boards = tmp_path / "boards.txt"
+    boards.write_text("1\n" + "!" * 16 + "\n")
+    r = subprocess.run([built.SOLVER_BIN, str(boards), str(tmp_path / "out.txt"), "60", "5"],
+                       cwd=str(tmp_path), capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0
+    assert "subboard.txt" in r.stderr and "value/value52" in r.stderr
 
 
 def test_cli_file_errors(built, tmp_path):
