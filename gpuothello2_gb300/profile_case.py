@@ -6,6 +6,11 @@
       to capture: `ncu ... -k regex:batched_kernel -s 1 -c 1 ...`)
   python -m gpuothello2_gb300.profile_case --int-peak
       prints the INT32 issue rates measured by libgpo_intpeak.so
+  python -m gpuothello2_gb300.profile_case --think [N] [DEPTH]
+      think mode: loads an evaluator of 13 patterns (5 to 12 squares) with
+      seeded random weights, runs N positions (seed 6, 24..34 empties) to
+      DEPTH plies twice and prints the second run's kernel time, positions/s
+      and nodes/s
 """
 import ctypes
 import os
@@ -27,9 +32,33 @@ def int_peak():
               flush=True)
 
 
+def think_case(n, depth):
+    import numpy as np
+
+    import gpuothello2_gb300 as g
+
+    # 4 rows, 2 diagonals, corner blocks, an edge with its X squares and
+    # shorter lines: 13 patterns of 5 to 12 squares
+    rows = [0xFF << (8 * r) for r in range(4)]
+    masks = rows + [0x8040201008040201, 0x0102040810204080, 0x1F1F, 0x070707, 0x42FF,
+                    0x0F0F0F, 0x1F, 0x804020100804, 0x3C3C]
+    rng = np.random.default_rng(1)
+    total = sum(3 ** bin(m).count("1") for m in masks)
+    g.eval_load(masks, rng.uniform(-4, 4, total), 0.5)
+    p, o = g.generate(6, n, 24, 34)
+    for _ in range(2):
+        _, _, nodes, st, _ = g.think(p, o, depth)
+    sec = st.kernel_ms / 1e3
+    print("think ok n=%d depth=%d kernel_ms=%.3f positions/s=%.4g nodes/s=%.4g" %
+          (n, depth, st.kernel_ms, n / sec, st.nodes / sec), flush=True)
+
+
 def main(argv):
     if argv and argv[0] == "--int-peak":
         int_peak()
+        return
+    if argv and argv[0] == "--think":
+        think_case(int(argv[1]) if len(argv) > 1 else 65536, int(argv[2]) if len(argv) > 2 else 6)
         return
     import gpuothello2_gb300 as g
 
