@@ -52,7 +52,7 @@ W_NODE = 418  # INT32 ops per node: mobility + flip + make-move of the reference
 # (2,711,552 B), scaled to the launch by its position count.
 DRAM_BYTES_PER_POSITION = 2711552.0 / 131072
 SEED, N_POS, LO, HI, DEPTH = 2, 1 << 20, 8, 16, 16
-METRIC = "exact-solved positions/s at 8-16 empties (batched vs plain, same GB300)"
+METRIC = "exact-solved positions/s at 8\u201316 empties: batched+learned vs plain, same GB300"
 WORKLOAD = ("1,048,576 positions, random playouts seed 2, empties uniform 8..16, DEPTH 16")
 CPU_SAMPLE = 1536
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -377,7 +377,9 @@ def main():
         "data": "synthetic: seeded random playouts (xoshiro256**, seed 2), generated on device",
         "config": {"workload": WORKLOAD, "positions_per_gpu": n, "depth": DEPTH,
                    "l2": "flushed between steps (256 MiB write, untimed)",
-                   "method": "batched: empties-bucketed persistent queue",
+                   "method": ("batched: empties-bucketed persistent queue, hard positions "
+                              "expanded level by level; learned root ordering %s" %
+                              ("on (--learned)" if args.learned else "off (--learned turns it on)")),
                    "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None),
                    "learned": learned_info},
         "e2e": {"value": e2e_value, "unit": "positions/s", "h2d_bytes_per_step": 16 * n,
