@@ -24,7 +24,9 @@ the timed region.
          cores, on a bounded sample of the same stream
 
 Options: `--learned` trains the MLP move orderer first (untimed) and orders
-the roots of positions with >= 14 empties with it; `--tuned` autotunes the
+the roots of positions with >= 14 empties with it; `--table` turns on the
+transposition table and reports its probes, hits, updates and 32-byte-sector
+traffic rate; `--tuned` autotunes the
 launch and search parameters on a sample of the batch first (untimed);
 `--plain` also times the plain kernel on the same batch.
 
@@ -212,6 +214,9 @@ def main():
                          "of positions with >= 14 empties with it")
     ap.add_argument("--learned-train", type=int, default=1 << 20,
                     help="training positions for --learned")
+    ap.add_argument("--table", action="store_true",
+                    help="use the transposition table (2^24 16-byte entries, nodes with >= 11 "
+                         "empties) and report its traffic")
     ap.add_argument("--tuned", action="store_true",
                     help="autotune launch/search parameters on a 4,096-position sample of the "
                          "batch first (untimed; cached per GPU, depth and empties range)")
@@ -271,9 +276,11 @@ def main():
 
     def solve_device(method):
         st = g.Stats()
+        batched = method == g.METHOD_BATCHED
         opt = g.options(method=method, split_min_empties=args.split,
-                        use_learned=1 if args.learned and method == g.METHOD_BATCHED else 0,
-                        **(tuned if method == g.METHOD_BATCHED else {}))
+                        use_learned=1 if args.learned and batched else 0,
+                        use_table=1 if args.table and batched else 0,
+                        **(tuned if batched else {}))
         rc = L.solve_batch_device(dp.data_ptr(), do.data_ptr(), n, DEPTH, ds.data_ptr(), None,
                                   None, ctypes.byref(opt), ctypes.byref(st), stream.cuda_stream)
         if rc != 0:
@@ -290,7 +297,8 @@ def main():
         """One step through the host-buffer entry point (pinned buffers):
         host->device copies, solve, device->host scores, wall clock."""
         opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split,
-                        use_learned=1 if args.learned else 0, **tuned)
+                        use_learned=1 if args.learned else 0, use_table=1 if args.table else 0,
+                        **tuned)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         rc = L.solve_batch_ex(hp.data_ptr(), ho.data_ptr(), n, DEPTH, hs.data_ptr(), None, None,
@@ -311,7 +319,7 @@ def main():
                 solve_device(method)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(steps)]
-        kern_ms, nodes, splits, launches = [], [], [], []
+        kern_ms, nodes, splits, launches, table = [], [], [], [], []
         barrier()
         if sampler:
             sampler.__enter__()
@@ -324,18 +332,31 @@ def main():
             nodes.append(st.nodes)
             splits.append(st.splits)
             launches.append(st.launches)
+            table.append((st.table_probes, st.table_hits, st.table_updates))
         barrier()
         if sampler:
             sampler.__exit__(None, None, None)
         step_ms = [a.elapsed_time(b) for a, b in ev]
         timed.splits = splits
         timed.launches = launches
+        timed.table = table
         return step_ms, kern_ms, nodes
 
     sampler = ClockSampler(local)
     e2e_t = []
     step_ms, kern_ms, nodes = timed(g.METHOD_BATCHED, args.warmup, args.steps, sampler, e2e_t)
     batched_splits, batched_launches = list(timed.splits), int(sum(timed.launches))
+    table_stats = None
+    if args.table:
+        probes = sum(t[0] for t in timed.table)
+        hits = sum(t[1] for t in timed.table)
+        updates = sum(t[2] for t in timed.table)
+        kern_s = sum(kern_ms) / 1000.0
+        # each probe reads and each update writes one 16-byte entry: 32-byte
+        # DRAM sectors either way
+        table_stats = {"probes": probes, "hits": hits, "updates": updates,
+                       "sector_bytes": 32 * (probes + updates),
+                       "gbs": 32 * (probes + updates) / kern_s / 1e9 if kern_s > 0 else None}
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world, dev)
     value = job_value(world, n, args.steps, total_s)
     scores = ds.cpu().numpy()
@@ -394,6 +415,7 @@ def main():
                      "nodes_per_launch": mean_nodes, "kernel_ms": 1000.0 * mean_kern_s},
         "nodes_per_s": mean_nodes / mean_kern_s,
         "splits_per_step": statistics.mean(batched_splits) if batched_splits else 0,
+        "table": table_stats,
         "cpu_baseline": cpu,
         "clocks": sampler.summary(),
         # counted by the library per call: bucketing (3) and the search per
