@@ -410,16 +410,24 @@ __global__ void scatter_lists_kernel(const u64* __restrict__ lists,
 Net g_infer;        // network loaded for the solver
 u64* g_lists_tmp = nullptr;
 bool g_loaded = false;
+// Guards g_infer / g_loaded: gpo_mlp_load may run on another thread while a
+// solve orders its roots.  (Freeing the network's buffers synchronises the
+// device, so kernels already enqueued finish before the memory goes.)
+std::mutex g_mlp_mutex;
 
 }  // namespace
 
-bool mlp_loaded() { return g_loaded; }
+bool mlp_loaded() {
+  std::lock_guard<std::mutex> lock(g_mlp_mutex);
+  return g_loaded;
+}
 
 // Root orders for the `count` positions d_idx[0..count) of d_player/d_opp:
 // d_lists[d_idx[i]] = packed list of the five best legal moves by logit.
 int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
                     u64* d_lists, cudaStream_t s, unsigned* launched) {
   *launched = 0;
+  std::lock_guard<std::mutex> lock(g_mlp_mutex);
   if (!g_loaded) return GPO_ERR_ARG;
   Net& t = g_infer;
   for (long off = 0; off < count; off += t.rows) {
@@ -439,10 +447,6 @@ int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx
 }  // namespace gpo
 
 using namespace gpo;
-
-namespace {
-std::mutex g_mlp_mutex;
-}
 
 extern "C" {
 
