@@ -4,7 +4,8 @@
   bin/solver             C++ CLI `solver INPUT OUTPUT DEPTH` over the C ABI
   bin/gen_boards         C++ board-file generator over the C ABI
   oracle/lib/liboracle.so  CPU oracle (test infrastructure, not the product)
-  oracle/lib/libthink_host.so  csrc/think.cuh compiled for the CPU (tests only)
+  oracle/lib/libthink_host.so, libbatched_emu.so  csrc/think.cuh and batched.cu
+                         compiled for the CPU (built on demand by the tests)
   oracle/_ref/refsolve, refthink  the reference's own search and think mode
                          built for the CPU, only where the reference sources
                          are present (x86-64)
@@ -31,8 +32,10 @@ SOLVER_BIN = os.path.join(BIN_DIR, "solver")
 GEN_BIN = os.path.join(BIN_DIR, "gen_boards")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "lib", "liboracle.so")
-# host build of csrc/think.cuh for the CPU tests (test infrastructure)
+# test infrastructure, built on demand by the CPU tests: csrc/think.cuh
+# compiled for the host, and batched.cu under the SIMT emulation
 THINK_HOST_LIB = os.path.join(ORACLE_DIR, "lib", "libthink_host.so")
+BATCHED_EMU_LIB = os.path.join(ORACLE_DIR, "lib", "libbatched_emu.so")
 REF_BIN = os.path.join(ORACLE_DIR, "_ref", "refsolve")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -130,6 +133,20 @@ def build_think_host():
     return THINK_HOST_LIB
 
 
+def build_batched_emu():
+    """tests/batched_emu.cpp: the batched search kernel's source run on CPU
+    threads (tests/simt/simt_prelude.h), for tests only."""
+    os.makedirs(os.path.dirname(BATCHED_EMU_LIB), exist_ok=True)
+    src = os.path.join(ROOT, "tests", "batched_emu.cpp")
+    simt = os.path.join(ROOT, "tests", "simt")
+    deps = [src, os.path.join(simt, "simt_prelude.h"), os.path.join(simt, "cuda_runtime.h")]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
+    if _stale(BATCHED_EMU_LIB, deps):
+        _run(["g++", "-std=c++20", "-O2", "-pthread", "-shared", "-fPIC", "-include",
+              os.path.join(simt, "simt_prelude.h"), "-I", simt, src, "-o", BATCHED_EMU_LIB])
+    return BATCHED_EMU_LIB
+
+
 def build_reference():
     """The reference's search compiled for the CPU (oracle/ref_build.sh);
     a no-op where the reference sources or an x86-64 host are absent."""
@@ -139,14 +156,12 @@ def build_reference():
 
 
 def build_all(verbose=False):
-    with ThreadPoolExecutor(4) as ex:
+    with ThreadPoolExecutor(3) as ex:
         f_lib = ex.submit(build_library, verbose)
         f_orc = ex.submit(build_oracle)
-        f_th = ex.submit(build_think_host)
         f_ref = ex.submit(build_reference)
         f_lib.result()
         f_orc.result()
-        f_th.result()
         f_ref.result()
     build_host()
 

@@ -101,9 +101,13 @@ __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
 }
 
 __device__ __forceinline__ unsigned long long global_ns() {
+#ifdef GPO_SIMT_EMU  // the CPU emulation of this kernel used by the tests
+  return gpo_emu_ns();
+#else
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+#endif
 }
 
 __device__ __forceinline__ unsigned pack_result(int v, int move) {

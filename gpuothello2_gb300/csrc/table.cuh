@@ -41,6 +41,9 @@ __device__ __forceinline__ TTKey tt_key(u64 P, u64 O) {
 
 __device__ __forceinline__ void tt_cas128(u64* addr, u64 c0, u64 c1, u64 v0, u64 v1, u64& o0,
                                           u64& o1) {
+#ifdef GPO_SIMT_EMU  // the CPU emulation of the search used by the tests
+  gpo_emu_cas128(addr, c0, c1, v0, v1, o0, o1);
+#else
   asm volatile(
       "{\n\t.reg .b128 c, v, d;\n\t"
       "mov.b128 c, {%2, %3};\n\t"
@@ -50,6 +53,7 @@ __device__ __forceinline__ void tt_cas128(u64* addr, u64 c0, u64 c1, u64 v0, u64
       : "=l"(o0), "=l"(o1)
       : "l"(c0), "l"(c1), "l"(v0), "l"(v1), "l"(addr)
       : "memory");
+#endif
 }
 
 __device__ __forceinline__ bool tt_same(const TTKey& k, int bits, u64 w0, u64 w1) {

@@ -1,0 +1,121 @@
+"""The batched search kernel's own source (csrc/batched.cu) run on CPU
+threads under the SIMT emulation (tests/batched_emu.cpp,
+tests/simt/simt_prelude.h) against the reference's golden scores and the
+oracle: the frame tiers, the ordering threshold, the transposition table,
+in-kernel donation between warps, node budgets and input rejection -- the
+code paths a GPU run takes, checked without a GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests.test_oracle import golden_ref
+
+OVERLAP, DEPTH, BUDGET = 2, 1, 4
+
+
+class EmuOptions(ctypes.Structure):
+    _fields_ = [("warps", ctypes.c_int), ("ff", ctypes.c_int), ("smem_slots", ctypes.c_int),
+                ("donate_min", ctypes.c_int), ("long_nodes", ctypes.c_uint64),
+                ("max_tasks", ctypes.c_uint), ("node_budget", ctypes.c_uint64),
+                ("budget_mark", ctypes.c_int), ("tt_bits", ctypes.c_int),
+                ("tt_min", ctypes.c_int), ("root_lists", ctypes.c_void_p),
+                ("learned_min", ctypes.c_int)]
+
+
+@pytest.fixture(scope="module")
+def emu(built):
+    L = ctypes.CDLL(built.build_batched_emu())
+    L.emu_batched.argtypes = ([ctypes.c_void_p] * 2 + [ctypes.c_int] * 2 +
+                              [ctypes.POINTER(EmuOptions)] + [ctypes.c_void_p] * 4)
+
+    def run(p, o, depth, **kw):
+        p = np.ascontiguousarray(p, np.uint64)
+        o = np.ascontiguousarray(o, np.uint64)
+        n = len(p)
+        score = np.zeros(n, np.int8)
+        best = np.zeros(n, np.int8)
+        nodes = np.zeros(n, np.uint64)
+        stats = np.zeros(7, np.uint64)
+        opt = EmuOptions(**{"warps": 1, **kw})
+        rc = L.emu_batched(p.ctypes.data, o.ctypes.data, n, depth, ctypes.byref(opt),
+                           score.ctypes.data, best.ctypes.data, nodes.ctypes.data,
+                           stats.ctypes.data)
+        assert rc == 0
+        return score, best, nodes, stats
+
+    return run
+
+
+@pytest.fixture(scope="module")
+def c1():
+    p, o, scores, _ = golden_ref("c1_seed0_e10")
+    return p[:48], o[:48], scores[:48]
+
+
+def test_scores_and_best_moves(emu, oracle, c1):
+    p, o, scores = c1
+    sc, bm, nodes, st = emu(p, o, 10, smem_slots=4)
+    assert np.array_equal(sc.astype(int), scores)
+    assert st[6] == 0 and st[0] == nodes.sum() and (nodes > 0).all()
+    # every best move reaches the score
+    for i in range(len(p)):
+        m = int(bm[i])
+        assert 0 <= m < 64
+        f = oracle.L.orc_flip(int(p[i]), int(o[i]), m)
+        assert f
+        cp, co = int(o[i]) ^ f, int(p[i]) ^ f ^ (1 << m)
+        v, _, _, _ = oracle.solve_batch(np.array([cp], np.uint64), np.array([co], np.uint64),
+                                        mode=1)
+        assert -int(v[0]) == int(sc[i])
+
+
+@pytest.mark.parametrize("ff,slots", [(8, 0), (11, 9)])
+def test_ordering_threshold_and_frame_tiers(emu, c1, ff, slots):
+    p, o, scores = c1
+    sc, _, _, st = emu(p, o, 16, ff=ff, smem_slots=slots)
+    assert np.array_equal(sc.astype(int), scores) and st[6] == 0
+
+
+def test_transposition_table(emu, c1):
+    p, o, scores = c1
+    sc, _, nodes, st = emu(p, o, 10, smem_slots=4, tt_bits=16, tt_min=6)
+    assert np.array_equal(sc.astype(int), scores) and st[6] == 0
+    probes, hits, updates = int(st[1]), int(st[2]), int(st[3])
+    assert probes > 0 and updates > 0 and hits <= probes
+
+
+def test_donation_between_warps(emu, oracle):
+    p, o = oracle.generate(11, 6, 13, 13)
+    want, _, _, _ = oracle.solve_batch(p, o, mode=1)
+    # 2 warps, 6 positions: idle lanes ask for subtrees; roots past 2048
+    # nodes hand moves out unasked
+    sc, _, nodes, st = emu(p, o, 13, warps=2, smem_slots=4, donate_min=8, long_nodes=2048)
+    assert np.array_equal(sc, want) and st[6] == 0
+    assert st[4] > 0  # subtrees handed out
+    assert st[0] == nodes.sum()
+
+
+def test_node_budget_marks_or_fails(emu, c1):
+    p, o, scores = c1
+    _, _, full_nodes, _ = emu(p, o, 10, smem_slots=4)
+    budget = int(np.median(full_nodes))
+    sc, _, _, st = emu(p, o, 10, smem_slots=4, node_budget=budget, budget_mark=1)
+    over = sc == -128
+    assert over.any() and (~over).any() and st[6] == 0
+    assert np.array_equal(sc[~over].astype(int), scores[~over])
+    assert (full_nodes[over] > budget).all()
+    _, _, _, st = emu(p, o, 10, smem_slots=4, node_budget=budget)
+    assert int(st[6]) & BUDGET
+
+
+def test_rejected_inputs(emu, c1):
+    p, o, scores = c1
+    p, o = p[:8].copy(), o[:8].copy()
+    p[3] |= np.uint64(int(o[3]) & -int(o[3]))  # a square in both bitboards
+    sc, _, _, st = emu(p, o, 10, smem_slots=4)
+    assert int(st[6]) & OVERLAP and sc[3] == 0
+    keep = np.arange(8) != 3
+    assert np.array_equal(sc[keep].astype(int), scores[:8][keep])
+    _, _, _, st = emu(p[keep], o[keep], 9, smem_slots=4)
+    assert int(st[6]) & DEPTH
