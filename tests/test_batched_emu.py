@@ -119,3 +119,38 @@ def test_rejected_inputs(emu, c1):
     assert np.array_equal(sc[keep].astype(int), scores[:8][keep])
     _, _, _, st = emu(p[keep], o[keep], 9, smem_slots=4)
     assert int(st[6]) & DEPTH
+
+
+def pack_root_list(moves, total):
+    """A root list as the learned orderer writes it (mlp.cu order_kernel):
+    up to five (slot << 6 | square) entries of 12 bits, unused entries all
+    ones, bit 63 set when the position has more legal moves than the list."""
+    lst = 0x0FFFFFFFFFFFFFFF
+    for slot, sq in enumerate(moves[:5]):
+        e = (slot << 6) | sq
+        lst = (lst & ~(0xFFF << (12 * slot))) | (e << (12 * slot))
+    if total > min(5, len(moves)):
+        lst |= 1 << 63
+    return lst
+
+
+@pytest.mark.parametrize("order", ["high_first", "best_first"])
+def test_learned_root_lists_keep_scores_exact(emu, oracle, c1, order):
+    p, o, scores = c1
+    lists = np.zeros(len(p), np.uint64)
+    used = 0
+    for i in range(len(p)):
+        legal = oracle.L.orc_mobility(int(p[i]), int(o[i]))
+        moves = [k for k in range(64) if (legal >> k) & 1]
+        if order == "high_first":
+            moves = moves[::-1]
+        else:  # the move the oracle finds best first
+            _, _, _, b = oracle.solve_batch(p[i:i + 1], o[i:i + 1], mode=1)
+            if 0 <= int(b[0]) < 64:
+                moves.remove(int(b[0]))
+                moves.insert(0, int(b[0]))
+        lists[i] = pack_root_list(moves, len(moves))
+        used += 1
+    sc, bm, _, st = emu(p, o, 10, smem_slots=4, root_lists=lists.ctypes.data, learned_min=10)
+    assert used == len(p)
+    assert np.array_equal(sc.astype(int), scores) and st[6] == 0
