@@ -14,6 +14,7 @@ Translation units are compiled in parallel; a unit is rebuilt only when a
 source it depends on (same directory headers included) is newer.
 """
 import os
+import re
 import shutil
 import subprocess
 import sys
@@ -145,6 +146,36 @@ def build_batched_emu():
         _run(["g++", "-std=c++20", "-O2", "-pthread", "-shared", "-fPIC", "-include",
               os.path.join(simt, "simt_prelude.h"), "-I", simt, src, "-o", BATCHED_EMU_LIB])
     return BATCHED_EMU_LIB
+
+
+PIPELINE_EMU_LIB = os.path.join(ORACLE_DIR, "lib", "libpipeline_emu.so")
+_LAUNCH = re.compile(r"(\w+)<<<(.*?)>>>\(")
+
+
+def build_pipeline_emu():
+    """tests/pipeline_emu.cpp: the C-ABI layer and every solve kernel run on
+    CPU threads (tests only).  prep.cu and plain.cu are copied into
+    oracle/lib/emu/ with their <<<...>>> launches rewritten to
+    simt_launch(kernel, simt_cfg(...), args)."""
+    emu_dir = os.path.join(ORACLE_DIR, "lib", "emu")
+    os.makedirs(emu_dir, exist_ok=True)
+    for name in ("prep.cu", "plain.cu"):
+        src = os.path.join(CSRC, name)
+        dst = os.path.join(emu_dir, name.replace(".cu", "_emu.cu"))
+        text = _LAUNCH.sub(r"simt_launch(\1, simt_cfg(\2), ", open(src).read())
+        if not os.path.exists(dst) or open(dst).read() != text:
+            with open(dst, "w") as f:
+                f.write(text)
+    src = os.path.join(ROOT, "tests", "pipeline_emu.cpp")
+    simt = os.path.join(ROOT, "tests", "simt")
+    deps = [src, os.path.join(simt, "simt_prelude.h"), os.path.join(simt, "cuda_runtime.h"),
+            os.path.join(ROOT, "include", "gpuothello2.h")]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
+    if _stale(PIPELINE_EMU_LIB, deps):
+        _run(["g++", "-std=c++20", "-O2", "-pthread", "-shared", "-fPIC", "-include",
+              os.path.join(simt, "simt_prelude.h"), "-I", simt, "-I", emu_dir, "-I", CSRC, src,
+              "-o", PIPELINE_EMU_LIB])
+    return PIPELINE_EMU_LIB
 
 
 def build_reference():

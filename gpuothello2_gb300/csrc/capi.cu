@@ -45,10 +45,14 @@ struct Context {
   DonatedTask* dQueue = nullptr;
   unsigned* dReady = nullptr;
   unsigned* dConsumed = nullptr;
-  unsigned* dPosTasks = nullptr;  // per input position (capacity cap)
+  unsigned* dPosTasks = nullptr;  // per position of a pass (capacity pass_cap)
   unsigned long long* dTable = nullptr;  // transposition table
   int table_bits = 0;
-  u64* dLists = nullptr;  // learned root orders (capacity cap)
+  u64* dLists = nullptr;  // learned root orders (capacity pass_cap)
+  // dPerm, dPosTasks and dLists hold one entry per position of a search
+  // pass; an expansion level can hold more positions than the call's input,
+  // so they grow on their own capacity, checked by every pass.
+  size_t pass_cap = 0;
   // second pass (hard positions)
   size_t second_cap = 0;
   unsigned* d2Idx = nullptr;
@@ -147,6 +151,7 @@ void free_buffers(Context* c) {
   c->dNodes = nullptr;
   c->dPerm = nullptr;
   c->cap = 0;
+  c->pass_cap = 0;
 }
 
 int ensure_context(Context** out) {
@@ -185,10 +190,28 @@ int ensure_capacity(Context* c, size_t n) {
   GPO_CK(cudaMalloc(&c->dScore, cap));
   GPO_CK(cudaMalloc(&c->dBest, cap));
   GPO_CK(cudaMalloc(&c->dNodes, cap * sizeof(unsigned long long)));
+  c->cap = cap;
+  return GPO_OK;
+}
+
+// Per-position scratch of one search pass (queue order, outstanding
+// subtrees, learned root orders) for n positions.  Called by every pass,
+// after the previous pass has finished with the arrays.
+int ensure_pass_scratch(Context* c, size_t n) {
+  if (n <= c->pass_cap) return GPO_OK;
+  cudaFree(c->dPerm);
+  cudaFree(c->dPosTasks);
+  cudaFree(c->dLists);
+  c->dPerm = nullptr;
+  c->dPosTasks = nullptr;
+  c->dLists = nullptr;
+  c->pass_cap = 0;
+  size_t cap = 1024;
+  while (cap < n) cap *= 2;
   GPO_CK(cudaMalloc(&c->dPerm, cap * sizeof(unsigned)));
   GPO_CK(cudaMalloc(&c->dPosTasks, cap * sizeof(unsigned)));
   GPO_CK(cudaMalloc(&c->dLists, cap * sizeof(u64)));
-  c->cap = cap;
+  c->pass_cap = cap;
   return GPO_OK;
 }
 
@@ -229,6 +252,8 @@ struct PassConfig {
 int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
              signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
              const PassConfig& pc, cudaStream_t s, PassResult* pr) {
+  const int rcs = ensure_pass_scratch(c, static_cast<size_t>(n));
+  if (rcs != GPO_OK) return rcs;
   GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
   GPO_CK(cudaMemsetAsync(c->dHist, 0, 65 * sizeof(unsigned), s));
   GPO_CK(launch_bucket(dP, dO, n, depth, c->dHist, c->dCursor, c->dPerm, c->dStats, c->sms, s));

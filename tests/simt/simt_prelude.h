@@ -102,6 +102,9 @@ inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
 inline int __ffs(int x) { return __builtin_ffs(x); }
 inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
+  return static_cast<unsigned long long>((static_cast<unsigned __int128>(a) * b) >> 64);
+}
 inline unsigned long long __brevll(unsigned long long x) {
   unsigned long long r = 0;
   for (int i = 0; i < 64; ++i) r |= ((x >> i) & 1ULL) << (63 - i);
@@ -155,4 +158,54 @@ inline void gpo_emu_cas128(unsigned long long* addr, unsigned long long c0, unsi
     addr[0] = v0;
     addr[1] = v1;
   }
+}
+
+// ---- kernel launches ----
+// Runs `body` as one block of `threads` CPU threads (block index `b` of a
+// grid of `grid`): each thread gets its thread index, its warp's barrier
+// and the block barrier.  Blocks of an ordinary launch run one after
+// another, so a kernel's static __shared__ arrays are the block's.
+#include <functional>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+inline void simt_run_block(unsigned b, unsigned grid, unsigned threads,
+                           const std::function<void()>& body) {
+  blockDim = {threads, 1, 1};
+  gridDim = {grid, 1, 1};
+  SimtBarrier block(static_cast<int>(threads));
+  simt_block = &block;
+  const unsigned warps = (threads + 31) / 32;
+  std::vector<std::unique_ptr<SimtBarrier>> bars;
+  std::vector<SimtWarp> ws(warps);
+  for (unsigned w = 0; w < warps; ++w) {
+    bars.emplace_back(new SimtBarrier(32));
+    ws[w].bar = bars.back().get();
+  }
+  std::vector<std::thread> ts;
+  for (unsigned t = 0; t < threads; ++t) {
+    ts.emplace_back([&, t] {
+      threadIdx = {t, 0, 0};
+      blockIdx = {b, 0, 0};
+      simt_warp = &ws[t / 32];
+      body();
+    });
+  }
+  for (auto& th : ts) th.join();
+}
+
+struct SimtCfg {
+  unsigned grid, block;
+};
+template <class G, class B, class... Rest>
+inline SimtCfg simt_cfg(G grid, B block, Rest...) {
+  return SimtCfg{static_cast<unsigned>(grid), static_cast<unsigned>(block)};
+}
+
+template <class... KP, class... A>
+inline void simt_launch(void (*kernel)(KP...), SimtCfg c, A&&... a) {
+  std::tuple<KP...> args(std::forward<A>(a)...);
+  for (unsigned b = 0; b < c.grid; ++b)
+    simt_run_block(b, c.grid, c.block, [&] { std::apply(kernel, args); });
 }

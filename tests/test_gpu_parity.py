@@ -50,6 +50,18 @@ def test_scores_match_reference(gpu, name, seed, count, lo, hi, depth, method):
         assert st.launches >= 4
 
 
+def test_expansion_levels_larger_than_the_input(gpu):
+    """A small node budget turns 40 positions into thousands of children over
+    several levels: every pass sizes its scratch for its own positions."""
+    p, o, scores, _ = golden_ref("c3_seed2_mixed")
+    small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 11
+    p, o, scores = p[small][:40], o[small][:40], scores[small][:40]
+    sc, best, _, st, _ = gpu.solve(p, o, 16, best=True, expand_budget=2000)
+    assert np.array_equal(sc.astype(int), scores)
+    assert st.splits > 1024
+    assert ((best >= 0) & (best <= 64)).all()
+
+
 @pytest.mark.parametrize("name,depth", [("c1_seed0_e10", 10), ("c3_seed2_mixed", 16),
                                         ("readme9", 10)])
 def test_plain_kernel_walks_reference_tree(gpu, oracle, name, depth):

@@ -1,0 +1,145 @@
+"""The library's whole solve pipeline -- C ABI, bucketing, batched and plain
+search kernels, expansion of hard positions into children and their
+combination, the allocation-free entry point, the generator -- compiled as
+host C++ and run on CPU threads (tests/pipeline_emu.cpp under the SIMT
+emulation), called through the same C ABI the product exports, against the
+reference's golden scores and the oracle.  No GPU is involved; this checks
+the pipeline's logic (the GPU tests check the real device)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import gpuothello2_gb300 as g
+from tests.test_oracle import golden_ref
+
+
+@pytest.fixture(scope="module")
+def emu(built):
+    L = ctypes.CDLL(built.build_pipeline_emu())
+    vp, i, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64
+    L.gpo_default_options.argtypes = [ctypes.POINTER(g.Options)]
+    L.gpo_default_options.restype = None
+    L.solve_batch_ex.argtypes = [vp, vp, i, i, vp, vp, vp, ctypes.POINTER(g.Options),
+                                 ctypes.POINTER(g.Stats)]
+    L.solve_batch_device_noalloc.argtypes = [vp, vp, i, i, vp, vp]
+    L.gpo_generate.argtypes = [u64, u64, i, i, i, vp, vp]
+    return L
+
+
+def solve(L, p, o, depth, **kw):
+    p = np.ascontiguousarray(p, np.uint64)
+    o = np.ascontiguousarray(o, np.uint64)
+    n = len(p)
+    score = np.zeros(n, np.int8)
+    best = np.zeros(n, np.int8)
+    nodes = np.zeros(n, np.uint64)
+    opt = g.Options()
+    L.gpo_default_options(ctypes.byref(opt))
+    opt.threads_per_block = 32
+    for k, v in kw.items():
+        setattr(opt, k, v)
+    st = g.Stats()
+    rc = L.solve_batch_ex(p.ctypes.data, o.ctypes.data, n, depth, score.ctypes.data,
+                          best.ctypes.data, nodes.ctypes.data, ctypes.byref(opt),
+                          ctypes.byref(st))
+    return rc, score, best, nodes, st
+
+
+def best_moves_reach_scores(oracle, p, o, score, best):
+    for i in range(len(p)):
+        m = int(best[i])
+        if m == g.MOVE_PASS:
+            cp, co = int(o[i]), int(p[i])
+        else:
+            assert 0 <= m < 64
+            f = oracle.L.orc_flip(int(p[i]), int(o[i]), m)
+            assert f
+            cp, co = int(o[i]) ^ f, int(p[i]) ^ f ^ (1 << m)
+        v, _, _, _ = oracle.solve_batch(np.array([cp], np.uint64), np.array([co], np.uint64),
+                                        mode=1)
+        assert -int(v[0]) == int(score[i]), i
+
+
+@pytest.fixture(scope="module")
+def c1():
+    p, o, scores, _ = golden_ref("c1_seed0_e10")
+    return p[:32], o[:32], scores[:32]
+
+
+def test_default_pass(emu, oracle, c1):
+    p, o, scores = c1
+    rc, sc, bm, nodes, st = solve(emu, p, o, 10)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores)
+    # bucketing (3), the search, the marking pass that finds nothing
+    assert st.launches == 5 and st.splits == 0
+    assert st.nodes == int(nodes.sum())
+    best_moves_reach_scores(oracle, p, o, sc, bm)
+
+
+def test_expansion_of_hard_positions(emu, oracle, c1):
+    p, o, scores = c1
+    rc, sc, bm, nodes, st = solve(emu, p, o, 10, expand_budget=3000)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores)
+    assert st.splits > 0            # child positions made
+    assert st.launches > 5          # further passes, expansion and combination
+    best_moves_reach_scores(oracle, p, o, sc, bm)
+
+
+def test_expansion_on_mixed_empties(emu):
+    p, o, scores, _ = golden_ref("c3_seed2_mixed")
+    small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 11
+    p, o, scores = p[small][:40], o[small][:40], scores[small][:40]
+    rc, sc, _, _, st = solve(emu, p, o, 16, expand_budget=2000, smem_frames=-1)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores) and st.splits > 0
+
+
+def test_plain_kernel_walks_reference_tree(emu, oracle, c1):
+    p, o, scores = c1
+    rc, sc, _, nodes, st = solve(emu, p, o, 10, method=g.METHOD_PLAIN)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores)
+    _, _, onodes, _ = oracle.solve_batch(p, o, 10, mode=0)
+    assert np.array_equal(nodes, onodes) and st.launches == 1
+
+
+@pytest.mark.parametrize("kw", [{"use_table": 1, "table_bits": 16, "table_min_empties": 6},
+                                {"split_min_empties": 8, "threads_per_block": 64},
+                                {"fastest_first_empties": 11, "smem_frames": 3}])
+def test_options_keep_scores_exact(emu, c1, kw):
+    p, o, scores = c1
+    rc, sc, _, _, st = solve(emu, p, o, 12, **kw)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores)
+    if "use_table" in kw:
+        assert st.table_probes > 0 and st.table_updates > 0
+
+
+def test_error_statuses(emu, c1):
+    p, o, scores = c1
+    assert solve(emu, p, o, 9)[0] == g.GPO_ERR_DEPTH
+    q = p.copy()
+    q[5] |= np.uint64(int(o[5]) & -int(o[5]))
+    rc, sc, _, _, _ = solve(emu, q, o, 10)
+    assert rc == g.GPO_ERR_BOARD
+    keep = np.arange(len(p)) != 5
+    assert np.array_equal(sc[keep].astype(int), scores[keep])
+    # a node budget without splitting fails instead of marking
+    assert solve(emu, p, o, 10, node_budget=500, split_min_empties=-1)[0] == g.GPO_ERR_TIMEOUT
+
+
+def test_allocation_free_entry_point(emu, c1):
+    p, o, scores = c1
+    p = np.ascontiguousarray(p, np.uint64)
+    o = np.ascontiguousarray(o, np.uint64)
+    sc = np.zeros(len(p), np.int8)
+    # device pointers are host pointers in the emulation
+    rc = emu.solve_batch_device_noalloc(p.ctypes.data, o.ctypes.data, len(p), 10,
+                                        sc.ctypes.data, None)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores)
+
+
+def test_generator_matches_oracle(emu, oracle):
+    p = np.zeros(500, np.uint64)
+    o = np.zeros(500, np.uint64)
+    assert emu.gpo_generate(2, 1000, 500, 8, 16, p.ctypes.data, o.ctypes.data) == 0
+    op, oo = oracle.generate(2, 500, 8, 16, first=1000)
+    assert np.array_equal(p, op) and np.array_equal(o, oo)
