@@ -143,3 +143,28 @@ def test_generator_matches_oracle(emu, oracle):
     assert emu.gpo_generate(2, 1000, 500, 8, 16, p.ctypes.data, o.ctypes.data) == 0
     op, oo = oracle.generate(2, 500, 8, 16, first=1000)
     assert np.array_equal(p, op) and np.array_equal(o, oo)
+
+
+def test_random_option_mixes(emu, oracle):
+    """Seeded random batches, depths and option mixes against the oracle."""
+    rng = np.random.default_rng(20261203)
+    for _ in range(8):
+        n = int(rng.integers(1, 24))
+        lo = int(rng.integers(1, 11))
+        hi = int(rng.integers(lo, 12))
+        depth = int(rng.integers(hi, hi + 6))
+        p, o = oracle.generate(int(rng.integers(100, 10000)), n, lo, hi)
+        want, _, _, _ = oracle.solve_batch(p, o, mode=1)
+        kw = {"threads_per_block": int(rng.choice([32, 64]))}
+        if rng.random() < 0.5:
+            kw["expand_budget"] = int(rng.choice([50, 300, 2000]))
+        if rng.random() < 0.3:
+            kw["split_min_empties"] = int(rng.choice([-1, 6, 9]))
+        if rng.random() < 0.3:
+            kw.update(use_table=1, table_bits=16, table_min_empties=int(rng.integers(4, 10)))
+        if rng.random() < 0.3:
+            kw["smem_frames"] = int(rng.choice([-1, 1, 3, 8]))
+        if rng.random() < 0.3:
+            kw["fastest_first_empties"] = int(rng.integers(4, 13))
+        rc, sc, _, _, _ = solve(emu, p, o, depth, **kw)
+        assert rc == 0 and np.array_equal(sc, want), (n, lo, hi, depth, kw)
