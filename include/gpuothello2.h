@@ -159,8 +159,7 @@ int solve_batch_device_noalloc(const uint64_t* d_player, const uint64_t* d_opp, 
                                int8_t* d_score, void* stream);
 
 /*
- * Learned move orderer (no counterpart in the reference: the north-star's
- * learned part).  An MLP 192 -> 256 -> 256 -> 64 over (side-to-move discs,
+ * Learned move orderer (no counterpart in the reference).  An MLP 192 -> 256 -> 256 -> 64 over (side-to-move discs,
  * other discs, legal moves) with BF16 tensor-core products and FP32
  * accumulation, trained on the GPU on best-move labels from
  * solve_batch_ex.  Weights are a flat FP32 array of gpo_mlp_param_count()
