@@ -51,6 +51,7 @@ class Options(ctypes.Structure):
         ("table_min_empties", ctypes.c_int),
         ("smem_frames", ctypes.c_int),
         ("expand_budget", ctypes.c_uint64),
+        ("expand_windows", ctypes.c_int),
     ]
 
 

@@ -15,6 +15,8 @@ caller's batch:
   expand_budget          the split threshold of hard positions: the node
                          budget after which a position is replaced by its
                          children in the next pass
+  expand_windows         how those children are searched: all with full
+                         windows, or principal variation first
 
 Search: coordinate descent from the library defaults, one parameter at a
 time, each candidate timed on the same sample (best of `repeats` runs).
@@ -35,6 +37,7 @@ DEFAULTS = {
     "smem_frames": 0,
     "fastest_first_empties": 9,
     "expand_budget": 1 << 22,
+    "expand_windows": 0,
 }
 
 SPACE = (
@@ -42,6 +45,7 @@ SPACE = (
     ("smem_frames", (0, -1)),
     ("fastest_first_empties", (8, 9, 10, 11)),
     ("expand_budget", (1 << 20, 1 << 22, 1 << 24)),
+    ("expand_windows", (0, 1)),
 )
 
 

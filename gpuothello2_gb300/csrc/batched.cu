@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
             busy = started = true;
             pos = p;
             task_mbox = kNoMbox;
-            alpha = -64;
-            beta = 64;
+            alpha = args.root_alpha ? args.root_alpha[p] : -64;
+            beta = args.root_beta ? args.root_beta[p] : 64;
           }
         } else if (args.donate_min > 0) {
           qidx = atomicAdd(&args.stats->dq_head, 1u);  // wait for a donated subtree

@@ -245,6 +245,8 @@ struct PassConfig {
   bool mark;                  // over budget: score -128 instead of an error
   bool split;                 // hand subtrees of hard positions to idle lanes
   bool clear_table;           // clear the transposition table first
+  const signed char* alpha = nullptr;  // per-position search windows (null = full)
+  const signed char* beta = nullptr;
 };
 
 // One batched pass over device arrays already in place: bucketing, learned
@@ -343,6 +345,8 @@ int run_pass(Context* c, const u64* dP, const u64* dO, int n, int depth, signed 
     a.tt_bits = bits;
     a.tt_min = o.table_min_empties > 0 ? o.table_min_empties : 11;
   }
+  a.root_alpha = pc.alpha;
+  a.root_beta = pc.beta;
   a.wait_limit_ns =
       static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 600000) * 1000000ULL;
   if (dNodes) GPO_CK(cudaMemsetAsync(dNodes, 0, static_cast<size_t>(n) * sizeof(u64), s));
@@ -376,10 +380,13 @@ int ensure_second(Context* c, size_t n) {
 }
 
 // One level of the expansion: positions, their results, and (below the
-// input level) their parent and move.
+// input level) their parent and move; with their search windows when the
+// level is searched with windows (null = full window).
 struct Level {
   const u64* P = nullptr;
   const u64* O = nullptr;
+  const signed char* alpha = nullptr;
+  const signed char* beta = nullptr;
   signed char* score = nullptr;
   signed char* best = nullptr;
   unsigned long long* nodes = nullptr;
@@ -395,9 +402,33 @@ struct Level {
   }
   template <class T>
   cudaError_t alloc(T** p, size_t count) {
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), (count ? count : 1) * sizeof(T));
     if (e == cudaSuccess) owned.push_back(*p);
     return e;
+  }
+};
+
+// Counters summed over every pass of a solve.
+struct Totals {
+  unsigned long long nodes = 0, probes = 0, hits = 0, updates = 0, learned = 0, splits = 0;
+  double ms = 0.0;
+  void add(const PassResult& r) {
+    nodes += r.hs.nodes;
+    probes += r.hs.tt_probes;
+    hits += r.hs.tt_hits;
+    updates += r.hs.tt_updates;
+    learned += r.learned;
+    ms += r.ms;
+  }
+  void write(gpo_stats* stats) const {
+    if (!stats) return;
+    stats->nodes = nodes;
+    stats->table_probes = probes;
+    stats->table_hits = hits;
+    stats->table_updates = updates;
+    stats->learned_calls = learned;
+    stats->splits = splits;
+    stats->kernel_ms = ms;
   }
 };
 
@@ -407,22 +438,26 @@ constexpr unsigned long long kLevelBudget = 1ULL << 22;
 // Hard positions (over kLevelBudget nodes) are replaced by their children,
 // solved as independent positions in the next pass (again with the budget,
 // except in the last level); values combine bottom-up as the max of the
-// children's negated exact scores.  No lane ever waits for another, and
-// every child is an ordinary full-window solve, so a hard position spreads
-// over 10x, 100x, ... lanes without the stale-window cost of splitting a
-// running search.
-int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
-                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
-                 gpo_stats* stats, cudaStream_t s) {
+// children's negated scores.  No lane ever waits for another, and every
+// child is an ordinary solve, so a hard position spreads over 10x, 100x,
+// ... lanes without the stale-window cost of splitting a running search.
+// With windows (dAlpha/dBeta), each position is searched with its window and
+// a child inherits its parent's window negated and swapped; the max of the
+// children's fail-soft values is then the parent's fail-soft value.
+int run_expanded(Context* c, const u64* dP, const u64* dO, int n, const signed char* dAlpha,
+                 const signed char* dBeta, int depth, signed char* dScore, signed char* dBest,
+                 unsigned long long* dNodes, const gpo_options& o, bool clear_table, Totals* t,
+                 cudaStream_t s) {
+  if (n == 0) return GPO_OK;
   Level lv[kExpandLevels];
   lv[0].P = dP;
   lv[0].O = dO;
+  lv[0].alpha = dAlpha;
+  lv[0].beta = dBeta;
   lv[0].score = dScore;
   lv[0].best = dBest;
   lv[0].nodes = dNodes;
   lv[0].n = n;
-  unsigned long long nodes = 0, probes = 0, hits = 0, updates = 0, learned = 0;
-  double ms = 0.0;
   int rc = GPO_OK;
   int last = 0;
   for (int k = 0; k < kExpandLevels; ++k) {
@@ -432,15 +467,12 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     pc.budget = final_level ? 0 : (o.expand_budget > 0 ? o.expand_budget : kLevelBudget);
     pc.mark = !final_level;
     pc.split = false;
-    pc.clear_table = k == 0;
+    pc.clear_table = clear_table && k == 0;
+    pc.alpha = L.alpha;
+    pc.beta = L.beta;
     PassResult r;
     rc = run_pass(c, L.P, L.O, L.n, depth, L.score, L.best, L.nodes, o, pc, s, &r);
-    nodes += r.hs.nodes;
-    probes += r.hs.tt_probes;
-    hits += r.hs.tt_hits;
-    updates += r.hs.tt_updates;
-    learned += r.learned;
-    ms += r.ms;
+    t->add(r);
     last = k;
     if (rc != GPO_OK || final_level) break;
     // over-budget positions of this level
@@ -456,15 +488,20 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     Level& C = lv[k + 1];
     const size_t cap = static_cast<size_t>(m) * 33;
     u64 *cP = nullptr, *cO = nullptr;
+    signed char *ca = nullptr, *cb = nullptr;
     GPO_CK(C.alloc(&cP, cap));
     GPO_CK(C.alloc(&cO, cap));
     GPO_CK(C.alloc(&C.parent, cap));
     GPO_CK(C.alloc(&C.move, cap));
     GPO_CK(C.alloc(&C.score, cap));
     if (L.nodes) GPO_CK(C.alloc(&C.nodes, cap));
+    if (L.alpha) {
+      GPO_CK(C.alloc(&ca, cap));
+      GPO_CK(C.alloc(&cb, cap));
+    }
     GPO_CK(cudaMemsetAsync(c->dCursor + 1, 0, sizeof(unsigned), s));
     GPO_CK(launch_expand(L.P, L.O, L.idx, L.m, cP, cO, C.parent, C.move, c->dCursor + 1,
-                         static_cast<unsigned>(cap), s));
+                         static_cast<unsigned>(cap), L.alpha, L.beta, ca, cb, s));
     c->launches += 1;
     unsigned cn = 0;
     GPO_CK(cudaMemcpyAsync(&cn, c->dCursor + 1, sizeof(cn), cudaMemcpyDeviceToHost, s));
@@ -472,7 +509,10 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     if (cn > cap) return GPO_ERR_INTERNAL;
     C.P = cP;
     C.O = cO;
+    C.alpha = ca;
+    C.beta = cb;
     C.n = static_cast<int>(cn);
+    t->splits += cn;
   }
   // combine from the deepest level up
   for (int k = last; k >= 1 && rc == GPO_OK; --k) {
@@ -485,17 +525,136 @@ int run_expanded(Context* c, const u64* dP, const u64* dO, int n, int depth, sig
     c->launches += 2;
   }
   GPO_CK(cudaStreamSynchronize(s));
-  if (stats) {
-    stats->nodes = nodes;
-    stats->table_probes = probes;
-    stats->table_hits = hits;
-    stats->table_updates = updates;
-    stats->learned_calls = learned;
-    stats->splits = 0;
-    for (int k = 1; k <= last; ++k) stats->splits += static_cast<unsigned long long>(lv[k].n);
-    stats->kernel_ms = ms;
-  }
   return rc;
+}
+
+// Principal-variation-first expansion (expand_windows = 1).  The first pass
+// is the default one; a hard position's children are then searched in the
+// order alpha-beta would use: the first child in fastest-first order with
+// a full window (A), which fixes a bound on the parent; the other children
+// with a null window around that bound (B), which only tells whether each
+// beats it; the children that do, again with the window above the bound
+// (C).  Each set is solved by run_expanded, so a hard child is expanded in
+// turn with its window.  The parent's value is the max over A, B and C of
+// the negated values of A and C (C's are exact, and a B child outside C is
+// worth no more than A's bound).
+int run_pvs(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+            signed char* dBest, unsigned long long* dNodes, const gpo_options& o, Totals* t,
+            cudaStream_t s) {
+  Level top;  // owns this function's buffers
+  PassConfig pc;
+  pc.budget = o.expand_budget > 0 ? o.expand_budget : kLevelBudget;
+  pc.mark = true;
+  pc.split = false;
+  pc.clear_table = true;
+  PassResult r;
+  int rc = run_pass(c, dP, dO, n, depth, dScore, dBest, dNodes, o, pc, s, &r);
+  t->add(r);
+  if (rc != GPO_OK) return rc;
+  unsigned* idx = nullptr;
+  GPO_CK(top.alloc(&idx, static_cast<size_t>(n)));
+  GPO_CK(launch_collect_marked(dScore, n, idx, c->dCursor, s));
+  c->launches += 1;
+  unsigned mu = 0;
+  GPO_CK(cudaMemcpyAsync(&mu, c->dCursor, sizeof(mu), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  const int m = static_cast<int>(mu);
+  if (m == 0) return GPO_OK;
+
+  // A: one first child per marked position; B: the others
+  const size_t capb = static_cast<size_t>(m) * 32;
+  u64 *aP, *aO, *bP, *bO;
+  unsigned *apar, *bpar;
+  unsigned char *amov, *bmov;
+  signed char *asc, *bsc, *bound, *ba, *bb;
+  unsigned long long *anod = nullptr, *bnod = nullptr;
+  GPO_CK(top.alloc(&aP, m));
+  GPO_CK(top.alloc(&aO, m));
+  GPO_CK(top.alloc(&apar, m));
+  GPO_CK(top.alloc(&amov, m));
+  GPO_CK(top.alloc(&asc, m));
+  GPO_CK(top.alloc(&bP, capb));
+  GPO_CK(top.alloc(&bO, capb));
+  GPO_CK(top.alloc(&bpar, capb));
+  GPO_CK(top.alloc(&bmov, capb));
+  GPO_CK(top.alloc(&bsc, capb));
+  GPO_CK(top.alloc(&ba, capb));
+  GPO_CK(top.alloc(&bb, capb));
+  GPO_CK(top.alloc(&bound, static_cast<size_t>(n)));
+  if (dNodes) {
+    GPO_CK(top.alloc(&anod, m));
+    GPO_CK(top.alloc(&bnod, capb));
+  }
+  GPO_CK(cudaMemsetAsync(c->dCursor + 1, 0, sizeof(unsigned), s));
+  GPO_CK(launch_expand_first(dP, dO, idx, m, aP, aO, apar, amov, bP, bO, bpar, bmov,
+                             c->dCursor + 1, static_cast<unsigned>(capb), s));
+  c->launches += 1;
+  unsigned nbu = 0;
+  GPO_CK(cudaMemcpyAsync(&nbu, c->dCursor + 1, sizeof(nbu), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  if (nbu > capb) return GPO_ERR_INTERNAL;
+  const int nb = static_cast<int>(nbu);
+  t->splits += static_cast<unsigned long long>(m) + nbu;
+
+  rc = run_expanded(c, aP, aO, m, nullptr, nullptr, depth, asc, nullptr, anod, o, false, t, s);
+  if (rc != GPO_OK) return rc;
+  GPO_CK(launch_pvs_bound(asc, apar, m, bound, s));
+  c->launches += 1;
+
+  int nc = 0;
+  u64 *cP = nullptr, *cO = nullptr;
+  unsigned* cpar = nullptr;
+  unsigned char* cmov = nullptr;
+  signed char *csc = nullptr, *ca = nullptr, *cb = nullptr;
+  unsigned long long* cnod = nullptr;
+  if (nb > 0) {
+    GPO_CK(launch_pvs_window(bpar, nb, bound, ba, bb, s));
+    c->launches += 1;
+    rc = run_expanded(c, bP, bO, nb, ba, bb, depth, bsc, nullptr, bnod, o, false, t, s);
+    if (rc != GPO_OK) return rc;
+    GPO_CK(top.alloc(&cP, nb));
+    GPO_CK(top.alloc(&cO, nb));
+    GPO_CK(top.alloc(&cpar, nb));
+    GPO_CK(top.alloc(&cmov, nb));
+    GPO_CK(top.alloc(&csc, nb));
+    GPO_CK(top.alloc(&ca, nb));
+    GPO_CK(top.alloc(&cb, nb));
+    if (dNodes) GPO_CK(top.alloc(&cnod, nb));
+    GPO_CK(cudaMemsetAsync(c->dCursor + 2, 0, sizeof(unsigned), s));
+    GPO_CK(launch_pvs_research(bP, bO, bpar, bmov, bsc, nb, bound, cP, cO, cpar, cmov, ca, cb,
+                               c->dCursor + 2, s));
+    c->launches += 1;
+    unsigned ncu = 0;
+    GPO_CK(cudaMemcpyAsync(&ncu, c->dCursor + 2, sizeof(ncu), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    nc = static_cast<int>(ncu);
+    t->splits += ncu;
+    rc = run_expanded(c, cP, cO, nc, ca, cb, depth, csc, nullptr, cnod, o, false, t, s);
+    if (rc != GPO_OK) return rc;
+  }
+
+  // The parent's value and move come from A and C only: a B child that did
+  // not beat the bound is worth at most the bound (its result is only a
+  // bound, so its move must not win a tie), and one that did is in C with
+  // its exact value.  B still adds its node counts (into a discarded max).
+  unsigned *acc = nullptr, *acc_b = nullptr;
+  GPO_CK(top.alloc(&acc, static_cast<size_t>(n)));
+  GPO_CK(cudaMemsetAsync(acc, 0, static_cast<size_t>(n) * sizeof(unsigned), s));
+  GPO_CK(launch_combine(asc, apar, amov, anod, m, acc, dNodes, s));
+  c->launches += 1;
+  if (nb > 0 && dNodes) {
+    GPO_CK(top.alloc(&acc_b, static_cast<size_t>(n)));
+    GPO_CK(launch_combine(bsc, bpar, bmov, bnod, nb, acc_b, dNodes, s));
+    c->launches += 1;
+  }
+  if (nc > 0) {
+    GPO_CK(launch_combine(csc, cpar, cmov, cnod, nc, acc, dNodes, s));
+    c->launches += 1;
+  }
+  GPO_CK(launch_finalize(idx, m, acc, dScore, dBest, s));
+  c->launches += 1;
+  GPO_CK(cudaStreamSynchronize(s));
+  return GPO_OK;
 }
 
 // Runs the solve pipeline on device arrays already in place.  Batched
@@ -529,7 +688,15 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
   // split_min_empties: 0 (default) = expand hard positions into their
   // children level by level; > 0 = hand subtrees of hard positions to idle
   // lanes inside the kernel (second pass); < 0 = one pass, no splitting.
-  if (o.split_min_empties == 0 && o.node_budget == 0) return run_expanded(c, dP, dO, n, depth, dScore, dBest, dNodes, o, stats, s);
+  if (o.split_min_empties == 0 && o.node_budget == 0) {
+    Totals t;
+    const int rc = o.expand_windows > 0
+                       ? run_pvs(c, dP, dO, n, depth, dScore, dBest, dNodes, o, &t, s)
+                       : run_expanded(c, dP, dO, n, nullptr, nullptr, depth, dScore, dBest, dNodes,
+                                      o, true, &t, s);
+    t.write(stats);
+    return rc;
+  }
   const bool split = o.split_min_empties > 0;
   const bool two_pass = split && o.node_budget == 0;
   PassConfig p1;

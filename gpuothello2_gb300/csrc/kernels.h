@@ -59,6 +59,10 @@ struct BatchedArgs {
   unsigned* ready;           // per record: ticket + 1 of the last fill
   unsigned* consumed;        // per record: ticket + 1 of the last read
   unsigned long long wait_limit_ns;  // deadline of the launch, from its start
+  // Search window of each input position (null = -64, 64).  A narrower
+  // window gives the fail-soft value: exact inside it, a bound outside.
+  const signed char* root_alpha;
+  const signed char* root_beta;
 };
 
 struct BatchedLaunch {
@@ -102,9 +106,29 @@ cudaError_t launch_scatter_scores(const signed char* sc, const signed char* best
 
 // Expansion of hard positions into their children and the bottom-up
 // combination of the children's exact scores (prep.cu).
+// pa/pb: search windows of the level's positions (null = full window);
+// ca/cb receive the children's windows (written only when pa is given).
 cudaError_t launch_expand(const u64* P, const u64* O, const unsigned* idx, int m, u64* cP, u64* cO,
                           unsigned* cparent, unsigned char* cmove, unsigned* counter, unsigned cap,
-                          cudaStream_t s);
+                          const signed char* pa, const signed char* pb, signed char* ca,
+                          signed char* cb, cudaStream_t s);
+// Principal-variation-first expansion: first children (set A, one per
+// marked position, at its slot) and the rest (set B); the parents' values
+// through A; B's null windows; the B children that beat the bound (set C,
+// with the window (-64, -bound)).
+cudaError_t launch_expand_first(const u64* P, const u64* O, const unsigned* idx, int m, u64* aP,
+                                u64* aO, unsigned* aparent, unsigned char* amove, u64* bP, u64* bO,
+                                unsigned* bparent, unsigned char* bmove, unsigned* counter,
+                                unsigned cap, cudaStream_t s);
+cudaError_t launch_pvs_bound(const signed char* ascore, const unsigned* aparent, int m,
+                             signed char* bound, cudaStream_t s);
+cudaError_t launch_pvs_window(const unsigned* bparent, int nb, const signed char* bound,
+                              signed char* ba, signed char* bb, cudaStream_t s);
+cudaError_t launch_pvs_research(const u64* bP, const u64* bO, const unsigned* bparent,
+                                const unsigned char* bmove, const signed char* bscore, int nb,
+                                const signed char* bound, u64* cP, u64* cO, unsigned* cparent,
+                                unsigned char* cmove, signed char* ca, signed char* cb,
+                                unsigned* counter, cudaStream_t s);
 cudaError_t launch_combine(const signed char* cscore, const unsigned* cparent,
                            const unsigned char* cmove, const unsigned long long* cnodes, int count,
                            unsigned* acc, unsigned long long* nodes, cudaStream_t s);

@@ -243,12 +243,16 @@ cudaError_t launch_scatter_scores(const signed char* sc, const signed char* best
 // ---- expansion of hard positions into their children ----
 // For each marked position idx[i] of a level: its children (after each
 // legal move, or the swapped position when it must pass) are appended to the
-// next level, with the parent's index and the move (64 = pass).
+// next level, with the parent's index and the move (64 = pass).  When the
+// level carries search windows (pa/pb), each child gets the negated,
+// swapped window (-pb, -pa) in ca/cb.
 __global__ void expand_kernel(const u64* __restrict__ P, const u64* __restrict__ O,
                               const unsigned* __restrict__ idx, int m, u64* __restrict__ cP,
                               u64* __restrict__ cO, unsigned* __restrict__ cparent,
                               unsigned char* __restrict__ cmove, unsigned* __restrict__ counter,
-                              unsigned cap) {
+                              unsigned cap, const signed char* __restrict__ pa,
+                              const signed char* __restrict__ pb, signed char* __restrict__ ca,
+                              signed char* __restrict__ cb) {
   __shared__ __align__(16) u64 rays[256];
   gpo_build_rays(rays);
   __syncthreads();
@@ -260,6 +264,12 @@ __global__ void expand_kernel(const u64* __restrict__ P, const u64* __restrict__
   const int cnt = moves ? popc(moves) : 1;
   const unsigned base = atomicAdd(counter, static_cast<unsigned>(cnt));
   if (base + cnt > cap) return;  // the host checks the counter against cap
+  if (pa) {
+    for (int k = 0; k < cnt; ++k) {
+      ca[base + k] = static_cast<signed char>(-pb[j]);
+      cb[base + k] = static_cast<signed char>(-pa[j]);
+    }
+  }
   if (!moves) {
     cP[base] = o;
     cO[base] = p;
@@ -303,11 +313,151 @@ __global__ void finalize_kernel(const unsigned* __restrict__ idx, int m,
   if (best) best[idx[i]] = static_cast<signed char>(a & 255u);
 }
 
+// ---- principal-variation-first expansion (the expand_windows option) ----
+// A marked position's children split in two: the first in fastest-first
+// order (fewest replies for the opponent, lowest square on ties; the pass
+// child when the position must pass) goes to set A at the parent's slot i,
+// the others to set B.  A is searched with a full window; B with a null
+// window around the value A gives the parent; only the B children that beat
+// it are searched again (set C) -- the order alpha-beta itself would use.
+__global__ void expand_first_kernel(const u64* __restrict__ P, const u64* __restrict__ O,
+                                    const unsigned* __restrict__ idx, int m,
+                                    u64* __restrict__ aP, u64* __restrict__ aO,
+                                    unsigned* __restrict__ aparent,
+                                    unsigned char* __restrict__ amove, u64* __restrict__ bP,
+                                    u64* __restrict__ bO, unsigned* __restrict__ bparent,
+                                    unsigned char* __restrict__ bmove,
+                                    unsigned* __restrict__ counter, unsigned cap) {
+  __shared__ __align__(16) u64 rays[256];
+  gpo_build_rays(rays);
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const unsigned j = idx[i];
+  const u64 p = P[j], o = O[j];
+  const u64 moves = gpo_mobility(p, o);
+  aparent[i] = j;
+  if (!moves) {
+    aP[i] = o;
+    aO[i] = p;
+    amove[i] = static_cast<unsigned char>(kMovePassDev);
+    return;
+  }
+  int first = -1, first_key = 99;
+  for (u64 t = moves; t; t &= t - 1) {
+    const int sq = ctz64(t);
+    const u64 bit = 1ULL << sq;
+    const u64 f = gpo_flip(p, o, sq, rays);
+    const int key = popc(gpo_mobility(o ^ f, p ^ f ^ bit));
+    if (key < first_key) {
+      first_key = key;
+      first = sq;
+    }
+  }
+  {
+    const u64 bit = 1ULL << first;
+    const u64 f = gpo_flip(p, o, first, rays);
+    aP[i] = o ^ f;
+    aO[i] = p ^ f ^ bit;
+    amove[i] = static_cast<unsigned char>(first);
+  }
+  const int rest = popc(moves) - 1;
+  if (rest == 0) return;
+  const unsigned base = atomicAdd(counter, static_cast<unsigned>(rest));
+  if (base + rest > cap) return;  // the host checks the counter against cap
+  int k = 0;
+  for (u64 t = moves & ~(1ULL << first); t; t &= t - 1, ++k) {
+    const int sq = ctz64(t);
+    const u64 bit = 1ULL << sq;
+    const u64 f = gpo_flip(p, o, sq, rays);
+    bP[base + k] = o ^ f;
+    bO[base + k] = p ^ f ^ bit;
+    bparent[base + k] = j;
+    bmove[base + k] = static_cast<unsigned char>(sq);
+  }
+}
+
+// bound[parent] = the parent's value through its first child (exact).
+__global__ void pvs_bound_kernel(const signed char* __restrict__ ascore,
+                                 const unsigned* __restrict__ aparent, int m,
+                                 signed char* __restrict__ bound) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) bound[aparent[i]] = static_cast<signed char>(-ascore[i]);
+}
+
+// The B children's windows: the null window (bound, bound + 1) of the
+// parent, negated and swapped.
+__global__ void pvs_window_kernel(const unsigned* __restrict__ bparent, int nb,
+                                  const signed char* __restrict__ bound,
+                                  signed char* __restrict__ ba, signed char* __restrict__ bb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int v = bound[bparent[i]];
+  ba[i] = static_cast<signed char>(-v - 1);
+  bb[i] = static_cast<signed char>(-v);
+}
+
+// B children that beat their parent's bound: gathered into set C with the
+// window (-64, -bound), the parent's (bound, 64).
+__global__ void pvs_research_kernel(const u64* __restrict__ bP, const u64* __restrict__ bO,
+                                    const unsigned* __restrict__ bparent,
+                                    const unsigned char* __restrict__ bmove,
+                                    const signed char* __restrict__ bscore, int nb,
+                                    const signed char* __restrict__ bound,
+                                    u64* __restrict__ cP, u64* __restrict__ cO,
+                                    unsigned* __restrict__ cparent,
+                                    unsigned char* __restrict__ cmove, signed char* __restrict__ ca,
+                                    signed char* __restrict__ cb, unsigned* __restrict__ counter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const unsigned j = bparent[i];
+  if (-static_cast<int>(bscore[i]) <= bound[j]) return;
+  const unsigned k = atomicAdd(counter, 1u);  // k < nb: one slot per B child at most
+  cP[k] = bP[i];
+  cO[k] = bO[i];
+  cparent[k] = j;
+  cmove[k] = bmove[i];
+  ca[k] = -64;
+  cb[k] = static_cast<signed char>(-bound[j]);
+}
+
+cudaError_t launch_expand_first(const u64* P, const u64* O, const unsigned* idx, int m, u64* aP,
+                                u64* aO, unsigned* aparent, unsigned char* amove, u64* bP, u64* bO,
+                                unsigned* bparent, unsigned char* bmove, unsigned* counter,
+                                unsigned cap, cudaStream_t s) {
+  expand_first_kernel<<<(m + 127) / 128, 128, 0, s>>>(P, O, idx, m, aP, aO, aparent, amove, bP, bO,
+                                                       bparent, bmove, counter, cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pvs_bound(const signed char* ascore, const unsigned* aparent, int m,
+                             signed char* bound, cudaStream_t s) {
+  pvs_bound_kernel<<<(m + 255) / 256, 256, 0, s>>>(ascore, aparent, m, bound);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pvs_window(const unsigned* bparent, int nb, const signed char* bound,
+                              signed char* ba, signed char* bb, cudaStream_t s) {
+  pvs_window_kernel<<<(nb + 255) / 256, 256, 0, s>>>(bparent, nb, bound, ba, bb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pvs_research(const u64* bP, const u64* bO, const unsigned* bparent,
+                                const unsigned char* bmove, const signed char* bscore, int nb,
+                                const signed char* bound, u64* cP, u64* cO, unsigned* cparent,
+                                unsigned char* cmove, signed char* ca, signed char* cb,
+                                unsigned* counter, cudaStream_t s) {
+  pvs_research_kernel<<<(nb + 255) / 256, 256, 0, s>>>(bP, bO, bparent, bmove, bscore, nb, bound,
+                                                       cP, cO, cparent, cmove, ca, cb, counter);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_expand(const u64* P, const u64* O, const unsigned* idx, int m, u64* cP, u64* cO,
                           unsigned* cparent, unsigned char* cmove, unsigned* counter, unsigned cap,
-                          cudaStream_t s) {
+                          const signed char* pa, const signed char* pb, signed char* ca,
+                          signed char* cb, cudaStream_t s) {
   expand_kernel<<<(m + 127) / 128, 128, 0, s>>>(P, O, idx, m, cP, cO, cparent, cmove, counter,
-                                                 cap);
+                                                 cap, pa, pb, ca, cb);
   return cudaGetLastError();
 }
 

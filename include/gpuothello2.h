@@ -77,6 +77,11 @@ typedef struct gpo_options {
                                  = none (every frame in the global frame array) */
   uint64_t expand_budget;     /* split_min_empties == 0: per-position node budget of each
                                  expansion level; 0 = 2^22 */
+  int expand_windows;         /* split_min_empties == 0: 0 = every child of a hard position
+                                 searched with a full window; 1 = principal variation
+                                 first: the first child in fastest-first order with a full
+                                 window, its siblings with a null window around the bound it
+                                 gives, and only the siblings that beat it searched again */
 } gpo_options;
 
 typedef struct gpo_stats {
