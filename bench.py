@@ -420,6 +420,7 @@ def main():
                      "kernel": "batched_kernel", "ops_per_node": W_NODE,
                      "nodes_per_launch": mean_nodes, "kernel_ms": 1000.0 * mean_kern_s},
         "nodes_per_s": mean_nodes / mean_kern_s,
+        "nodes_per_position": mean_nodes / n,
         "splits_per_step": statistics.mean(batched_splits) if batched_splits else 0,
         "table": table_stats,
         "cpu_baseline": cpu,
