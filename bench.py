@@ -217,9 +217,9 @@ def main():
     ap.add_argument("--table", action="store_true",
                     help="use the transposition table (2^24 16-byte entries, nodes with >= 11 "
                          "empties) and report its traffic")
-    ap.add_argument("--windows", action="store_true",
-                    help="principal-variation-first expansion of hard positions "
-                         "(expand_windows = 1)")
+    ap.add_argument("--windows", type=int, default=0, choices=[0, 1, 2],
+                    help="principal-variation-first expansion of hard positions: 1 = at the "
+                         "top level, 2 = at every expanded position (expand_windows)")
     ap.add_argument("--tuned", action="store_true",
                     help="autotune launch/search parameters on a 4,096-position sample of the "
                          "batch first (untimed; cached per GPU, depth and empties range)")
@@ -283,7 +283,7 @@ def main():
         opt = g.options(method=method, split_min_empties=args.split,
                         use_learned=1 if args.learned and batched else 0,
                         use_table=1 if args.table and batched else 0,
-                        expand_windows=1 if args.windows and batched else 0,
+                        expand_windows=args.windows if batched else 0,
                         **(tuned if batched else {}))
         rc = L.solve_batch_device(dp.data_ptr(), do.data_ptr(), n, DEPTH, ds.data_ptr(), None,
                                   None, ctypes.byref(opt), ctypes.byref(st), stream.cuda_stream)
@@ -302,7 +302,7 @@ def main():
         host->device copies, solve, device->host scores, wall clock."""
         opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split,
                         use_learned=1 if args.learned else 0, use_table=1 if args.table else 0,
-                        expand_windows=1 if args.windows else 0, **tuned)
+                        expand_windows=args.windows, **tuned)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         rc = L.solve_batch_ex(hp.data_ptr(), ho.data_ptr(), n, DEPTH, hs.data_ptr(), None, None,
@@ -406,7 +406,7 @@ def main():
                               "expanded level by level; learned root ordering %s" %
                               ("on (--learned)" if args.learned else "off (--learned turns it on)"))
                    + ("; children of hard positions searched principal variation first "
-                      "(--windows)" if args.windows else ""),
+                      "(--windows %d)" % args.windows if args.windows else ""),
                    "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None),
                    "learned": learned_info},
         "e2e": {"value": e2e_value, "unit": "positions/s", "h2d_bytes_per_step": 16 * n,

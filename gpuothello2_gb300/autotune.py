@@ -16,7 +16,8 @@ caller's batch:
                          budget after which a position is replaced by its
                          children in the next pass
   expand_windows         how those children are searched: all with full
-                         windows, or principal variation first
+                         windows, or principal variation first (at the top
+                         level, or at every expanded position)
 
 Search: coordinate descent from the library defaults, one parameter at a
 time, each candidate timed on the same sample (best of `repeats` runs).
@@ -45,7 +46,7 @@ SPACE = (
     ("smem_frames", (0, -1)),
     ("fastest_first_empties", (8, 9, 10, 11)),
     ("expand_budget", (1 << 20, 1 << 22, 1 << 24)),
-    ("expand_windows", (0, 1)),
+    ("expand_windows", (0, 1, 2)),
 )
 
 

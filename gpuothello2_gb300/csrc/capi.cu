@@ -657,6 +657,160 @@ int run_pvs(Context* c, const u64* dP, const u64* dO, int n, int depth, signed c
   return GPO_OK;
 }
 
+// Recursive principal-variation-first expansion (expand_windows = 2): every
+// expanded position, at every level, searches its first child before its
+// siblings.  A position (with its window) gets one budgeted pass; if it is
+// marked, its first child is solved by this same function with the
+// position's window negated and swapped, which gives a bound; a bound at or
+// above beta cuts the position off (its siblings are never searched, as in
+// alpha-beta at a cut node); otherwise the siblings get the null window
+// above a' = max(alpha, bound), and when the position's window is wider than
+// that (a PV-type node), the siblings that beat a' are searched again for
+// their values.  Each of these sets recurses one level deeper; the last
+// level is searched without a budget.  The position's fail-soft value is the
+// max over its first child, the siblings (see pvs_siblings_kernel for which
+// of them count) and the re-searched ones.
+int run_pvs_rec(Context* c, const u64* dP, const u64* dO, int n, const signed char* dAlpha,
+                const signed char* dBeta, int depth, signed char* dScore, signed char* dBest,
+                unsigned long long* dNodes, const gpo_options& o, int level, bool clear_table,
+                Totals* t, cudaStream_t s) {
+  if (n == 0) return GPO_OK;
+  const bool final_level = level >= kExpandLevels - 1;
+  PassConfig pc;
+  pc.budget = final_level ? 0 : (o.expand_budget > 0 ? o.expand_budget : kLevelBudget);
+  pc.mark = !final_level;
+  pc.split = false;
+  pc.clear_table = clear_table;
+  pc.alpha = dAlpha;
+  pc.beta = dBeta;
+  PassResult r;
+  int rc = run_pass(c, dP, dO, n, depth, dScore, dBest, dNodes, o, pc, s, &r);
+  t->add(r);
+  if (rc != GPO_OK || final_level) return rc;
+
+  Level mem;  // owns this level's buffers
+  unsigned* idx = nullptr;
+  GPO_CK(mem.alloc(&idx, static_cast<size_t>(n)));
+  GPO_CK(launch_collect_marked(dScore, n, idx, c->dCursor, s));
+  c->launches += 1;
+  unsigned mu = 0;
+  GPO_CK(cudaMemcpyAsync(&mu, c->dCursor, sizeof(mu), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  const int m = static_cast<int>(mu);
+  if (m == 0) return GPO_OK;
+
+  // first children (A, at the parent's slot) and their siblings (B)
+  const size_t capb = static_cast<size_t>(m) * 32;
+  u64 *aP, *aO, *bP, *bO;
+  unsigned *apar, *bpar;
+  unsigned char *amov, *bmov;
+  signed char *asc, *bound, *aa = nullptr, *ab = nullptr;
+  unsigned long long *anod = nullptr;
+  GPO_CK(mem.alloc(&aP, m));
+  GPO_CK(mem.alloc(&aO, m));
+  GPO_CK(mem.alloc(&apar, m));
+  GPO_CK(mem.alloc(&amov, m));
+  GPO_CK(mem.alloc(&asc, m));
+  GPO_CK(mem.alloc(&bP, capb));
+  GPO_CK(mem.alloc(&bO, capb));
+  GPO_CK(mem.alloc(&bpar, capb));
+  GPO_CK(mem.alloc(&bmov, capb));
+  GPO_CK(mem.alloc(&bound, static_cast<size_t>(n)));
+  if (dNodes) GPO_CK(mem.alloc(&anod, m));
+  GPO_CK(cudaMemsetAsync(c->dCursor + 1, 0, sizeof(unsigned), s));
+  GPO_CK(launch_expand_first(dP, dO, idx, m, aP, aO, apar, amov, bP, bO, bpar, bmov,
+                             c->dCursor + 1, static_cast<unsigned>(capb), s));
+  c->launches += 1;
+  unsigned nbu = 0;
+  GPO_CK(cudaMemcpyAsync(&nbu, c->dCursor + 1, sizeof(nbu), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  if (nbu > capb) return GPO_ERR_INTERNAL;
+  const int nb = static_cast<int>(nbu);
+  t->splits += static_cast<unsigned long long>(m);
+  if (dAlpha) {
+    GPO_CK(mem.alloc(&aa, m));
+    GPO_CK(mem.alloc(&ab, m));
+    GPO_CK(launch_child_window(apar, m, dAlpha, dBeta, aa, ab, s));
+    c->launches += 1;
+  }
+  rc = run_pvs_rec(c, aP, aO, m, aa, ab, depth, asc, nullptr, anod, o, level + 1, false, t, s);
+  if (rc != GPO_OK) return rc;
+  GPO_CK(launch_pvs_bound(asc, apar, m, bound, s));
+  c->launches += 1;
+
+  // siblings with null windows, then the re-searches
+  int ns = 0, nc = 0;
+  u64 *sP = nullptr, *sO = nullptr, *cP = nullptr, *cO = nullptr;
+  unsigned *spar = nullptr, *cpar = nullptr;
+  unsigned char *smov = nullptr, *sflag = nullptr, *sskip = nullptr, *cmov = nullptr;
+  signed char *ssc = nullptr, *sa = nullptr, *sb = nullptr, *csc = nullptr, *ca = nullptr,
+              *cb = nullptr;
+  unsigned long long *snod = nullptr, *cnod = nullptr;
+  if (nb > 0) {
+    GPO_CK(mem.alloc(&sP, nb));
+    GPO_CK(mem.alloc(&sO, nb));
+    GPO_CK(mem.alloc(&spar, nb));
+    GPO_CK(mem.alloc(&smov, nb));
+    GPO_CK(mem.alloc(&ssc, nb));
+    GPO_CK(mem.alloc(&sa, nb));
+    GPO_CK(mem.alloc(&sb, nb));
+    GPO_CK(mem.alloc(&sflag, nb));
+    GPO_CK(mem.alloc(&sskip, nb));
+    if (dNodes) GPO_CK(mem.alloc(&snod, nb));
+    GPO_CK(cudaMemsetAsync(c->dCursor + 2, 0, sizeof(unsigned), s));
+    GPO_CK(launch_pvs_siblings(bP, bO, bpar, bmov, nb, dAlpha, dBeta, bound, sP, sO, spar, smov,
+                               sa, sb, sflag, sskip, c->dCursor + 2, s));
+    c->launches += 1;
+    unsigned nsu = 0;
+    GPO_CK(cudaMemcpyAsync(&nsu, c->dCursor + 2, sizeof(nsu), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+    ns = static_cast<int>(nsu);
+    t->splits += nsu;
+    rc = run_pvs_rec(c, sP, sO, ns, sa, sb, depth, ssc, nullptr, snod, o, level + 1, false, t, s);
+    if (rc != GPO_OK) return rc;
+    if (ns > 0) {
+      GPO_CK(mem.alloc(&cP, ns));
+      GPO_CK(mem.alloc(&cO, ns));
+      GPO_CK(mem.alloc(&cpar, ns));
+      GPO_CK(mem.alloc(&cmov, ns));
+      GPO_CK(mem.alloc(&csc, ns));
+      GPO_CK(mem.alloc(&ca, ns));
+      GPO_CK(mem.alloc(&cb, ns));
+      if (dNodes) GPO_CK(mem.alloc(&cnod, ns));
+      GPO_CK(cudaMemsetAsync(c->dCursor + 3, 0, sizeof(unsigned), s));
+      GPO_CK(launch_pvs_research2(sP, sO, spar, smov, ssc, sflag, ns, dAlpha, dBeta, bound, cP, cO,
+                                  cpar, cmov, ca, cb, c->dCursor + 3, s));
+      c->launches += 1;
+      unsigned ncu = 0;
+      GPO_CK(cudaMemcpyAsync(&ncu, c->dCursor + 3, sizeof(ncu), cudaMemcpyDeviceToHost, s));
+      GPO_CK(cudaStreamSynchronize(s));
+      nc = static_cast<int>(ncu);
+      t->splits += ncu;
+      rc = run_pvs_rec(c, cP, cO, nc, ca, cb, depth, csc, nullptr, cnod, o, level + 1, false, t,
+                       s);
+      if (rc != GPO_OK) return rc;
+    }
+  }
+
+  unsigned* acc = nullptr;
+  GPO_CK(mem.alloc(&acc, static_cast<size_t>(n)));
+  GPO_CK(cudaMemsetAsync(acc, 0, static_cast<size_t>(n) * sizeof(unsigned), s));
+  GPO_CK(launch_combine(asc, apar, amov, anod, m, acc, dNodes, s));
+  c->launches += 1;
+  if (ns > 0) {
+    GPO_CK(launch_combine_masked(ssc, spar, smov, snod, sskip, ns, acc, dNodes, s));
+    c->launches += 1;
+  }
+  if (nc > 0) {
+    GPO_CK(launch_combine(csc, cpar, cmov, cnod, nc, acc, dNodes, s));
+    c->launches += 1;
+  }
+  GPO_CK(launch_finalize(idx, m, acc, dScore, dBest, s));
+  c->launches += 1;
+  GPO_CK(cudaStreamSynchronize(s));
+  return GPO_OK;
+}
+
 // Runs the solve pipeline on device arrays already in place.  Batched
 // method: a first pass gives every position a node budget; the few hard
 // positions that exceed it are solved again in a second pass in which idle
@@ -690,10 +844,15 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
   // lanes inside the kernel (second pass); < 0 = one pass, no splitting.
   if (o.split_min_empties == 0 && o.node_budget == 0) {
     Totals t;
-    const int rc = o.expand_windows > 0
-                       ? run_pvs(c, dP, dO, n, depth, dScore, dBest, dNodes, o, &t, s)
-                       : run_expanded(c, dP, dO, n, nullptr, nullptr, depth, dScore, dBest, dNodes,
-                                      o, true, &t, s);
+    int rc;
+    if (o.expand_windows >= 2)
+      rc = run_pvs_rec(c, dP, dO, n, nullptr, nullptr, depth, dScore, dBest, dNodes, o, 0, true,
+                       &t, s);
+    else if (o.expand_windows == 1)
+      rc = run_pvs(c, dP, dO, n, depth, dScore, dBest, dNodes, o, &t, s);
+    else
+      rc = run_expanded(c, dP, dO, n, nullptr, nullptr, depth, dScore, dBest, dNodes, o, true, &t,
+                        s);
     t.write(stats);
     return rc;
   }

@@ -129,6 +129,31 @@ cudaError_t launch_pvs_research(const u64* bP, const u64* bO, const unsigned* bp
                                 const signed char* bound, u64* cP, u64* cO, unsigned* cparent,
                                 unsigned char* cmove, signed char* ca, signed char* cb,
                                 unsigned* counter, cudaStream_t s);
+// Recursive principal-variation-first expansion: children's windows from
+// their parents' (null = full); siblings of first children with null windows
+// (cut parents skipped; flag = parent needs a re-search); the flagged
+// siblings that beat the bound, with the window above it; and the
+// siblings' combination (node counts always, values unless skip[i]; see
+// pvs_siblings_kernel in prep.cu for when a sibling's value is left out).
+cudaError_t launch_child_window(const unsigned* cparent, int count, const signed char* pa,
+                                const signed char* pb, signed char* ca, signed char* cb,
+                                cudaStream_t s);
+cudaError_t launch_pvs_siblings(const u64* bP, const u64* bO, const unsigned* bparent,
+                                const unsigned char* bmove, int nb, const signed char* pa,
+                                const signed char* pb, const signed char* bound, u64* oP, u64* oO,
+                                unsigned* opar, unsigned char* omove, signed char* oa,
+                                signed char* ob, unsigned char* oflag, unsigned char* oskip,
+                                unsigned* counter, cudaStream_t s);
+cudaError_t launch_pvs_research2(const u64* sP, const u64* sO, const unsigned* spar,
+                                 const unsigned char* smove, const signed char* sscore,
+                                 const unsigned char* sflag, int ns, const signed char* pa,
+                                 const signed char* pb, const signed char* bound, u64* cP, u64* cO,
+                                 unsigned* cpar, unsigned char* cmove, signed char* ca,
+                                 signed char* cb, unsigned* counter, cudaStream_t s);
+cudaError_t launch_combine_masked(const signed char* cscore, const unsigned* cparent,
+                                  const unsigned char* cmove, const unsigned long long* cnodes,
+                                  const unsigned char* skip, int count, unsigned* acc,
+                                  unsigned long long* nodes, cudaStream_t s);
 cudaError_t launch_combine(const signed char* cscore, const unsigned* cparent,
                            const unsigned char* cmove, const unsigned long long* cnodes, int count,
                            unsigned* acc, unsigned long long* nodes, cudaStream_t s);

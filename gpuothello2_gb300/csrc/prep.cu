@@ -421,6 +421,152 @@ __global__ void pvs_research_kernel(const u64* __restrict__ bP, const u64* __res
   cb[k] = static_cast<signed char>(-bound[j]);
 }
 
+// ---- recursive principal-variation-first expansion (expand_windows = 2) ----
+// Windows of a parent (pa/pb, null = -64/64) as seen from its children.
+__device__ __forceinline__ int window_lo(const signed char* pa, unsigned j) {
+  return pa ? pa[j] : -64;
+}
+__device__ __forceinline__ int window_hi(const signed char* pb, unsigned j) {
+  return pb ? pb[j] : 64;
+}
+
+// ca/cb[i] = the window of child i: its parent's window negated and swapped.
+__global__ void child_window_kernel(const unsigned* __restrict__ cparent, int count,
+                                    const signed char* __restrict__ pa,
+                                    const signed char* __restrict__ pb, signed char* __restrict__ ca,
+                                    signed char* __restrict__ cb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const unsigned j = cparent[i];
+  ca[i] = static_cast<signed char>(-window_hi(pb, j));
+  cb[i] = static_cast<signed char>(-window_lo(pa, j));
+}
+
+// The siblings of first children: skipped when the first child already cut
+// the parent off (bound >= beta); the others get the null window above
+// a' = max(alpha, bound), and flag[k] = 1 when the parent's window is wider
+// than that null window (a sibling that beats a' must then be searched
+// again for its value).  skip[k] = 1 when the sibling's result must stay out
+// of the parent's max: its parent is re-searched and a' = bound, so the
+// sibling is worth at most the first child's value unless its re-search
+// says otherwise (a bound tying the first child must not supply the move).
+// When a' = alpha > bound the parent fails low and every sibling's upper
+// bound has to count.
+__global__ void pvs_siblings_kernel(const u64* __restrict__ bP, const u64* __restrict__ bO,
+                                    const unsigned* __restrict__ bparent,
+                                    const unsigned char* __restrict__ bmove, int nb,
+                                    const signed char* __restrict__ pa,
+                                    const signed char* __restrict__ pb,
+                                    const signed char* __restrict__ bound, u64* __restrict__ oP,
+                                    u64* __restrict__ oO, unsigned* __restrict__ opar,
+                                    unsigned char* __restrict__ omove, signed char* __restrict__ oa,
+                                    signed char* __restrict__ ob, unsigned char* __restrict__ oflag,
+                                    unsigned char* __restrict__ oskip,
+                                    unsigned* __restrict__ counter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const unsigned j = bparent[i];
+  const int lo = window_lo(pa, j), hi = window_hi(pb, j), b = bound[j];
+  if (b >= hi) return;
+  const int a2 = b > lo ? b : lo;
+  const unsigned k = atomicAdd(counter, 1u);  // k < nb
+  oP[k] = bP[i];
+  oO[k] = bO[i];
+  opar[k] = j;
+  omove[k] = bmove[i];
+  oa[k] = static_cast<signed char>(-a2 - 1);
+  ob[k] = static_cast<signed char>(-a2);
+  oflag[k] = hi > a2 + 1 ? 1 : 0;
+  oskip[k] = hi > a2 + 1 && b >= lo ? 1 : 0;
+}
+
+// Flagged siblings that beat a': searched again with the window (a', beta)
+// of the parent, i.e. (-beta, -a') for the child.
+__global__ void pvs_research2_kernel(const u64* __restrict__ sP, const u64* __restrict__ sO,
+                                     const unsigned* __restrict__ spar,
+                                     const unsigned char* __restrict__ smove,
+                                     const signed char* __restrict__ sscore,
+                                     const unsigned char* __restrict__ sflag, int ns,
+                                     const signed char* __restrict__ pa,
+                                     const signed char* __restrict__ pb,
+                                     const signed char* __restrict__ bound, u64* __restrict__ cP,
+                                     u64* __restrict__ cO, unsigned* __restrict__ cpar,
+                                     unsigned char* __restrict__ cmove, signed char* __restrict__ ca,
+                                     signed char* __restrict__ cb, unsigned* __restrict__ counter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns || !sflag[i]) return;
+  const unsigned j = spar[i];
+  const int lo = window_lo(pa, j), hi = window_hi(pb, j), b = bound[j];
+  const int a2 = b > lo ? b : lo;
+  if (-static_cast<int>(sscore[i]) <= a2) return;
+  const unsigned k = atomicAdd(counter, 1u);  // k < ns
+  cP[k] = sP[i];
+  cO[k] = sO[i];
+  cpar[k] = j;
+  cmove[k] = smove[i];
+  ca[k] = static_cast<signed char>(-hi);
+  cb[k] = static_cast<signed char>(-a2);
+}
+
+// combine_kernel for siblings: node counts always, values only for the
+// unflagged ones (a flagged sibling's value comes from its re-search, or is
+// a bound no better than the first child's).
+__global__ void combine_masked_kernel(const signed char* __restrict__ cscore,
+                                      const unsigned* __restrict__ cparent,
+                                      const unsigned char* __restrict__ cmove,
+                                      const unsigned long long* __restrict__ cnodes,
+                                      const unsigned char* __restrict__ skip, int count,
+                                      unsigned* __restrict__ acc,
+                                      unsigned long long* __restrict__ nodes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  if (!skip[i]) {
+    const int v = -static_cast<int>(cscore[i]);
+    atomicMax(&acc[cparent[i]], (static_cast<unsigned>(v + 128) << 8) | cmove[i]);
+  }
+  if (nodes && cnodes) atomicAdd(&nodes[cparent[i]], cnodes[i]);
+}
+
+cudaError_t launch_child_window(const unsigned* cparent, int count, const signed char* pa,
+                                const signed char* pb, signed char* ca, signed char* cb,
+                                cudaStream_t s) {
+  child_window_kernel<<<(count + 255) / 256, 256, 0, s>>>(cparent, count, pa, pb, ca, cb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pvs_siblings(const u64* bP, const u64* bO, const unsigned* bparent,
+                                const unsigned char* bmove, int nb, const signed char* pa,
+                                const signed char* pb, const signed char* bound, u64* oP, u64* oO,
+                                unsigned* opar, unsigned char* omove, signed char* oa,
+                                signed char* ob, unsigned char* oflag, unsigned char* oskip,
+                                unsigned* counter, cudaStream_t s) {
+  pvs_siblings_kernel<<<(nb + 255) / 256, 256, 0, s>>>(bP, bO, bparent, bmove, nb, pa, pb, bound,
+                                                       oP, oO, opar, omove, oa, ob, oflag, oskip,
+                                                       counter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pvs_research2(const u64* sP, const u64* sO, const unsigned* spar,
+                                 const unsigned char* smove, const signed char* sscore,
+                                 const unsigned char* sflag, int ns, const signed char* pa,
+                                 const signed char* pb, const signed char* bound, u64* cP, u64* cO,
+                                 unsigned* cpar, unsigned char* cmove, signed char* ca,
+                                 signed char* cb, unsigned* counter, cudaStream_t s) {
+  pvs_research2_kernel<<<(ns + 255) / 256, 256, 0, s>>>(sP, sO, spar, smove, sscore, sflag, ns,
+                                                        pa, pb, bound, cP, cO, cpar, cmove, ca,
+                                                        cb, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_combine_masked(const signed char* cscore, const unsigned* cparent,
+                                  const unsigned char* cmove, const unsigned long long* cnodes,
+                                  const unsigned char* skip, int count, unsigned* acc,
+                                  unsigned long long* nodes, cudaStream_t s) {
+  combine_masked_kernel<<<(count + 255) / 256, 256, 0, s>>>(cscore, cparent, cmove, cnodes, skip,
+                                                            count, acc, nodes);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_expand_first(const u64* P, const u64* O, const unsigned* idx, int m, u64* aP,
                                 u64* aO, unsigned* aparent, unsigned char* amove, u64* bP, u64* bO,
                                 unsigned* bparent, unsigned char* bmove, unsigned* counter,

@@ -81,7 +81,10 @@ typedef struct gpo_options {
                                  searched with a full window; 1 = principal variation
                                  first: the first child in fastest-first order with a full
                                  window, its siblings with a null window around the bound it
-                                 gives, and only the siblings that beat it searched again */
+                                 gives, and only the siblings that beat it searched again;
+                                 2 = the same at every expanded position, recursively, with
+                                 the siblings of a position cut off by its first child never
+                                 searched */
 } gpo_options;
 
 typedef struct gpo_stats {

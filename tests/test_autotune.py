@@ -15,7 +15,7 @@ def synthetic_cost(params):
     t += {0: 0.5, -1: 0.0}[params["smem_frames"]]
     t += abs(params["fastest_first_empties"] - 10) * 0.25
     t += {1 << 20: 0.0, 1 << 22: 0.1, 1 << 24: 0.2}[params["expand_budget"]]
-    t += {0: 0.05, 1: 0.0}[params["expand_windows"]]
+    t += {0: 0.05, 1: 0.0, 2: 0.02}[params["expand_windows"]]
     return t
 
 

@@ -25,10 +25,11 @@ def best_moves_reach_scores(oracle, p, o, score, best):
         assert -int(v[0]) == int(score[i])
 
 
-@pytest.mark.parametrize("budget", [2000, 1 << 16])
-def test_windowed_expansion_matches_reference(gpu, oracle, budget):
+@pytest.mark.parametrize("mode,budget", [(1, 2000), (1, 1 << 16), (2, 1 << 16)])
+def test_windowed_expansion_matches_reference(gpu, oracle, mode, budget):
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
-    sc, best, _, st, _ = gpu.solve(p, o, 16, best=True, expand_budget=budget, expand_windows=1)
+    sc, best, _, st, _ = gpu.solve(p, o, 16, best=True, expand_budget=budget,
+                                   expand_windows=mode)
     assert np.array_equal(sc.astype(int), scores)
     assert st.splits > 0
     sel = np.arange(0, len(p), 8)
@@ -39,6 +40,7 @@ def test_windowed_expansion_uses_fewer_nodes(gpu):
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
     full = gpu.solve(p, o, 16, expand_budget=1 << 16)[3]
     win = gpu.solve(p, o, 16, expand_budget=1 << 16, expand_windows=1)[3]
-    print("nodes: full-window children %d, windowed %d (%.3f)" %
-          (full.nodes, win.nodes, win.nodes / full.nodes))
-    assert win.nodes < full.nodes
+    rec = gpu.solve(p, o, 16, expand_budget=1 << 16, expand_windows=2)[3]
+    print("nodes: full-window children %d, windowed %d (%.3f), recursive %d (%.3f)" %
+          (full.nodes, win.nodes, win.nodes / full.nodes, rec.nodes, rec.nodes / full.nodes))
+    assert win.nodes < full.nodes and rec.nodes < full.nodes

@@ -170,14 +170,16 @@ def test_random_option_mixes(emu, oracle):
         assert rc == 0 and np.array_equal(sc, want), (n, lo, hi, depth, kw)
 
 
-def test_windowed_expansion_is_exact_and_smaller(emu, oracle):
-    """expand_windows = 1 (principal variation first): same scores, optimal
-    best moves, and fewer nodes than full-window children."""
+@pytest.mark.parametrize("mode", [1, 2])
+def test_windowed_expansion_is_exact_and_smaller(emu, oracle, mode):
+    """expand_windows = 1 (principal variation first at the top) and 2 (at
+    every expanded position): same scores, optimal best moves, fewer nodes
+    than full-window children."""
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
     small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 10
     p, o, scores = p[small][:32], o[small][:32], scores[small][:32]
     _, _, _, _, full = solve(emu, p, o, 16, expand_budget=500)
-    rc, sc, bm, nodes, st = solve(emu, p, o, 16, expand_budget=500, expand_windows=1)
+    rc, sc, bm, nodes, st = solve(emu, p, o, 16, expand_budget=500, expand_windows=mode)
     assert rc == 0 and np.array_equal(sc.astype(int), scores)
     best_moves_reach_scores(oracle, p, o, sc, bm)
     assert st.nodes == int(nodes.sum())
@@ -192,7 +194,8 @@ def test_windowed_expansion_random_batches(emu, oracle):
         hi = int(rng.integers(lo, 12))
         p, o = oracle.generate(int(rng.integers(100, 10000)), n, lo, hi)
         want, _, _, _ = oracle.solve_batch(p, o, mode=1)
-        kw = {"expand_windows": 1, "expand_budget": int(rng.choice([30, 200, 1500]))}
+        kw = {"expand_windows": int(rng.choice([1, 2])),
+              "expand_budget": int(rng.choice([30, 200, 1500]))}
         if rng.random() < 0.4:
             kw.update(use_table=1, table_bits=16, table_min_empties=6)
         rc, sc, bm, _, _ = solve(emu, p, o, hi + int(rng.integers(0, 4)), **kw)
