@@ -18,6 +18,8 @@ caller's batch:
   expand_windows         how those children are searched: all with full
                          windows, or principal variation first (at the top
                          level, or at every expanded position)
+  use_table              the transposition table (2^24 entries), which also
+                         carries work between the expansion's passes
 
 Search: coordinate descent from the library defaults, one parameter at a
 time, each candidate timed on the same sample (best of `repeats` runs).
@@ -39,6 +41,7 @@ DEFAULTS = {
     "fastest_first_empties": 9,
     "expand_budget": 1 << 22,
     "expand_windows": 0,
+    "use_table": 0,
 }
 
 SPACE = (
@@ -47,6 +50,7 @@ SPACE = (
     ("fastest_first_empties", (8, 9, 10, 11)),
     ("expand_budget", (1 << 20, 1 << 22, 1 << 24)),
     ("expand_windows", (0, 1, 2)),
+    ("use_table", (0, 1)),
 )
 
 
