@@ -32,7 +32,9 @@ struct Context {
   unsigned long long* dNodes = nullptr;
   unsigned* dPerm = nullptr;
   unsigned* dHist = nullptr;    // 65 buckets
-  unsigned* dCursor = nullptr;  // 65 buckets
+  // 65 bucket cursors during bucketing; between passes, [0] counts marked
+  // positions and [1..3] the children sets of an expansion
+  unsigned* dCursor = nullptr;
   DeviceStats* dStats = nullptr;
   unsigned char* dFrames = nullptr;  // batched kernel's global frame slots
   size_t frames_cap = 0;
