@@ -45,13 +45,13 @@ class Options(ctypes.Structure):
         ("fastest_first_empties", ctypes.c_int),
         ("learned_min_empties", ctypes.c_int),
         ("node_budget", ctypes.c_uint64),
-        ("split_min_empties", ctypes.c_int),
+        ("help_min_empties", ctypes.c_int),
         ("wait_limit_ms", ctypes.c_int),
         ("table_bits", ctypes.c_int),
         ("table_min_empties", ctypes.c_int),
         ("smem_frames", ctypes.c_int),
-        ("expand_budget", ctypes.c_uint64),
-        ("expand_windows", ctypes.c_int),
+        ("stability_min_empties", ctypes.c_int),
+        ("roots_per_warp", ctypes.c_int),
     ]
 
 
@@ -66,6 +66,7 @@ class Stats(ctypes.Structure):
         ("kernel_ms", ctypes.c_double),
         ("total_ms", ctypes.c_double),
         ("launches", ctypes.c_uint64),
+        ("stability_cuts", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -134,38 +134,48 @@ def build_think_host():
     return THINK_HOST_LIB
 
 
+_LAUNCH = re.compile(r"(\w+)<<<(.*?)>>>\(")
+
+
+def _emu_sources():
+    """Copies of the kernel files with their <<<...>>> launches rewritten to
+    simt_launch(kernel, simt_cfg(...), args), in oracle/lib/emu/."""
+    emu_dir = os.path.join(ORACLE_DIR, "lib", "emu")
+    os.makedirs(emu_dir, exist_ok=True)
+    for name in ("batched.cu", "prep.cu", "plain.cu"):
+        src = os.path.join(CSRC, name)
+        dst = os.path.join(emu_dir, name.replace(".cu", "_emu.cu"))
+        text = _LAUNCH.sub(r"simt_launch(\1, simt_cfg(\2), ", open(src).read())
+        text = text.replace('#include "', '#include "%s/' % CSRC)
+        if not os.path.exists(dst) or open(dst).read() != text:
+            with open(dst, "w") as f:
+                f.write(text)
+    return emu_dir
+
+
 def build_batched_emu():
     """tests/batched_emu.cpp: the batched search kernel's source run on CPU
     threads (tests/simt/simt_prelude.h), for tests only."""
     os.makedirs(os.path.dirname(BATCHED_EMU_LIB), exist_ok=True)
+    emu_dir = _emu_sources()
     src = os.path.join(ROOT, "tests", "batched_emu.cpp")
     simt = os.path.join(ROOT, "tests", "simt")
     deps = [src, os.path.join(simt, "simt_prelude.h"), os.path.join(simt, "cuda_runtime.h")]
     deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
     if _stale(BATCHED_EMU_LIB, deps):
         _run(["g++", "-std=c++20", "-O2", "-pthread", "-shared", "-fPIC", "-include",
-              os.path.join(simt, "simt_prelude.h"), "-I", simt, src, "-o", BATCHED_EMU_LIB])
+              os.path.join(simt, "simt_prelude.h"), "-I", simt, "-I", emu_dir, src, "-o",
+              BATCHED_EMU_LIB])
     return BATCHED_EMU_LIB
 
 
 PIPELINE_EMU_LIB = os.path.join(ORACLE_DIR, "lib", "libpipeline_emu.so")
-_LAUNCH = re.compile(r"(\w+)<<<(.*?)>>>\(")
 
 
 def build_pipeline_emu():
     """tests/pipeline_emu.cpp: the C-ABI layer and every solve kernel run on
-    CPU threads (tests only).  prep.cu and plain.cu are copied into
-    oracle/lib/emu/ with their <<<...>>> launches rewritten to
-    simt_launch(kernel, simt_cfg(...), args)."""
-    emu_dir = os.path.join(ORACLE_DIR, "lib", "emu")
-    os.makedirs(emu_dir, exist_ok=True)
-    for name in ("prep.cu", "plain.cu"):
-        src = os.path.join(CSRC, name)
-        dst = os.path.join(emu_dir, name.replace(".cu", "_emu.cu"))
-        text = _LAUNCH.sub(r"simt_launch(\1, simt_cfg(\2), ", open(src).read())
-        if not os.path.exists(dst) or open(dst).read() != text:
-            with open(dst, "w") as f:
-                f.write(text)
+    CPU threads (tests only), from the rewritten copies of _emu_sources."""
+    emu_dir = _emu_sources()
     src = os.path.join(ROOT, "tests", "pipeline_emu.cpp")
     simt = os.path.join(ROOT, "tests", "simt")
     deps = [src, os.path.join(simt, "simt_prelude.h"), os.path.join(simt, "cuda_runtime.h"),

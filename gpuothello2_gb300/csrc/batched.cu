@@ -1,39 +1,63 @@
 // Batched solver: one persistent launch over a device work queue of
-// positions ordered by empty count (most empties first); one lane searches
-// one position at a time and refills itself from the queue when done.
+// positions ordered by empty count (most empties first).  A lane searches
+// one position at a time and refills itself from the queue; when the queue
+// is empty (or the warp already holds its quota of positions) idle lanes
+// help the busy lanes of their own warp with their positions.
 //
-// Uniform-step engine.  Thread-per-board search diverges because lanes sit
-// at different kinds of nodes.  Here every loop iteration does the same
-// heavy work in every lane -- one flip and one mobility:
+// Search (values identical to the reference's negamax, solver.cu:15-283;
+// the tree differs):
+//   - fail-soft principal-variation search: the first move of a node gets
+//     the node's window, later moves a null window just above the best value
+//     so far, and a move that beats it is searched again with the window
+//     above it;
+//   - move order: nodes with >= ff empties play their moves by fewest
+//     opponent replies (corners first on ties) from a packed five-entry list
+//     (the role of the reference's sorted UpperNode list, solver.cu:78-93);
+//     below ff, corners, then squares of odd-parity quadrants, avoiding
+//     X-squares;
+//   - transposition table (table.cuh) at nodes with >= tt_min empties: a
+//     probe when the node is created (a bound outside the window closes it,
+//     one inside narrows the window) and a bound stored when it closes;
+//   - stability cutoff at nodes with >= stab_min empties: discs of the
+//     opponent that can never flip cap the side to move's score at
+//     64 - 2 * stable, which closes a node whose alpha is at or above it;
+//   - a move at a node with two empties scores its child (one empty) in the
+//     same step: the child's last move needs only a flip count;
+//   - passes happen in place with the window negated and swapped
+//     (solver.cu:57-73, 214-221, 246-256 semantics).
 //
-//   op INIT    mobility of a new root
-//   op MOVE    play square sq: flip, child position, child mobility; the
-//              child is pushed (or scored at once when it fills the board)
-//   op PASS    the side to move has no move: child = swapped position and
-//              its mobility (no mobility there either = game over)
-//   op KEY     ordering probe at a fastest-first node: the opponent's
-//              mobility after square sq becomes that move's sort key
-//   op REMASK  mobility of the current node again, to search the moves that
-//              did not fit in its five-entry ordered list
-//
-// and only cheap bookkeeping diverges: choosing the op, returning finished
-// nodes to their parents (a short loop of frame pops), inserting keys.
-//
-// Search (values identical to the reference's negamax, tree different):
-// fail-soft alpha-beta; nodes with >= ff empties search their moves in
-// fastest-first order (fewest opponent replies, corners first on ties), the
-// role of the reference's sorted UpperNode list (solver.cu:78-93); nodes
-// below ff use corner/parity order from the move mask.  Passes happen in
-// place with the window negated and swapped (solver.cu:57-73, 214-221,
-// 246-256 semantics).
+// Uniform step.  Every loop iteration every lane does at most one move flip
+// plus one mobility (or, at nodes with two empties, one or two more flips):
+// a move (the child is pushed), a fastest-first ordering probe, a root init,
+// a pass, a re-mask, or a handed-out move.  Only the bookkeeping around it
+// diverges.  The loop keeps one copy of the flip and of the mobility code,
+// and the rare paths (table, stability, split-node search) out of line: the
+// hot loop's instruction footprint decides how often warps wait for
+// instruction fetch.
 //
 // Frames: a node with E empties saves {move word, flips of the move being
 // searched, packed alpha/beta/best/square/flags} in slot E when it pushes a
-// child.  The move word is the remaining-move mask, or at fastest-first
-// nodes the packed ordered list (search.cuh), so no per-thread local memory
-// is used.  Slots 2..smem_top are in shared memory, interleaved by thread
-// ([slot][thread]: a warp touches 32 consecutive words); the rarely touched
-// slots above smem_top are in a per-lane global array (L2-resident).
+// child; a node with two empties never pushes, so slots run 3..depth.  All
+// slots live in shared memory, interleaved by thread ([slot][thread]), when
+// they fit, else in a per-lane global array.  Bit 0 of the flips word (A1,
+// a corner, which is never flipped) records that the child is being
+// searched again after beating a null window.
+//
+// Helping (young brothers wait, inside one warp).  A lane may offer one of
+// its nodes as a split node: >= help_min empties, not passed, first move
+// searched (that is the "young brothers wait" condition), window still open,
+// moves left in its frame.  While the owner is below that node, idle lanes
+// of the warp receive its untried moves, one per idle lane and iteration;
+// the owner lane itself takes each move from its own frame, so the frame has
+// one writer.  A helper searches the child with a null window above the
+// node's best value, searches it again with the window above its result when
+// it beats that bound, and reports the value with atomicMax into the owner's
+// result word (value, exactness, move) and a count of outstanding moves.  An
+// owner closes its split node only after every handed-out move has reported;
+// a cutoff (or an abort) at the node raises a flag that makes its helpers
+// abandon their subtrees.  Helpers may split their own nodes in turn.  All
+// waiting is between lanes of one warp inside one loop, so it always ends;
+// a launch deadline still bounds everything.
 #include "common.cuh"
 #include "kernels.h"
 #include "search.cuh"
@@ -43,11 +67,12 @@ namespace gpo {
 
 namespace {
 
-enum : int { OP_NONE = 0, OP_INIT, OP_MOVE, OP_PASS, OP_KEY, OP_REMASK, OP_DONATE };
+enum : int { OP_NONE = 0, OP_INIT, OP_MOVE, OP_PASS, OP_KEY, OP_REMASK, OP_HAND };
 enum : int { PH_INIT = 0, PH_MASK, PH_KEY, PH_LIST };
 
-constexpr int kFrameBytes = 20;
 constexpr int kRayBytes = 256 * 8;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr u64 kResearch = 1ULL;  // flips-word flag: the child is a re-search
 
 __device__ __forceinline__ unsigned pack_meta(int sq, int alpha, int beta, int best, int passed,
                                               int list) {
@@ -55,50 +80,140 @@ __device__ __forceinline__ unsigned pack_meta(int sq, int alpha, int beta, int b
          (static_cast<unsigned>(beta & 0xff) << 14) | (static_cast<unsigned>(best & 0xff) << 22) |
          (static_cast<unsigned>(passed) << 30) | (static_cast<unsigned>(list) << 31);
 }
+__device__ __forceinline__ int meta_sq(unsigned x) { return static_cast<int>(x & 63u); }
+__device__ __forceinline__ int meta_alpha(unsigned x) {
+  return static_cast<signed char>((x >> 6) & 0xff);
+}
+__device__ __forceinline__ int meta_beta(unsigned x) {
+  return static_cast<signed char>((x >> 14) & 0xff);
+}
+__device__ __forceinline__ int meta_best(unsigned x) {
+  return static_cast<signed char>((x >> 22) & 0xff);
+}
+__device__ __forceinline__ int meta_passed(unsigned x) { return static_cast<int>((x >> 30) & 1u); }
+__device__ __forceinline__ int meta_list(unsigned x) { return static_cast<int>(x >> 31); }
 
+// Helper results: (value + 128) << 9 | exact << 8 | move; 0 = none.  The
+// max prefers the higher value, then an exact value over a bound.
+__device__ __forceinline__ unsigned pack_acc(int v, int exact, int move) {
+  return (static_cast<unsigned>(v + 128) << 9) | (static_cast<unsigned>(exact) << 8) |
+         static_cast<unsigned>(move & 255);
+}
+__device__ __forceinline__ int acc_value(unsigned a) { return static_cast<int>(a >> 9) - 128; }
+
+// Frame slots 3..depth of one lane: all in shared memory ([slot][thread])
+// when they fit beside the launch's occupancy, else all in the global frame
+// array ([slot][grid thread], L1-cached).  One address formula for both,
+// used through generic loads and stores.
 struct Frames {
-  u64* sM;
-  u64* sF;
-  unsigned* sX;
-  u64* gM;
-  u64* gF;
-  unsigned* gX;
-  int B, t, top;
-  size_t G, gid;
+  u64* m;            // M word of slot E: m[E * stride + off]
+  u64* f;            // F words, same indexing
+  unsigned* x;       // X words, same indexing
+  long long stride;  // threads the slots are interleaved over
+  long long off;     // this thread's index minus 3 * stride
 
-  __device__ __forceinline__ void store(int E, u64 m, u64 f, unsigned x) const {
-    if (E <= top) {
-      const int i = (E - 2) * B + t;
-      sM[i] = m;
-      sF[i] = f;
-      sX[i] = x;
-    } else {
-      const size_t i = static_cast<size_t>(E - top - 1) * G + gid;
-      gM[i] = m;
-      gF[i] = f;
-      gX[i] = x;
-    }
+  __device__ __forceinline__ long long idx(int E) const { return E * stride + off; }
+  __device__ __forceinline__ u64* m_ptr(int E) const { return m + idx(E); }
+  __device__ __forceinline__ u64* f_ptr(int E) const { return f + idx(E); }
+  __device__ __forceinline__ void store(int E, u64 mv, u64 fv, unsigned xv) const {
+    const long long i = idx(E);
+    m[i] = mv;
+    f[i] = fv;
+    x[i] = xv;
   }
-  __device__ __forceinline__ void load(int E, u64& m, u64& f, unsigned& x) const {
-    if (E <= top) {
-      const int i = (E - 2) * B + t;
-      m = sM[i];
-      f = sF[i];
-      x = sX[i];
-    } else {
-      const size_t i = static_cast<size_t>(E - top - 1) * G + gid;
-      m = gM[i];
-      f = gF[i];
-      x = gX[i];
-    }
+  __device__ __forceinline__ void load(int E, u64& mv, u64& fv, unsigned& xv) const {
+    const long long i = idx(E);
+    mv = m[i];
+    fv = f[i];
+    xv = x[i];
   }
 };
 
-}  // namespace
+// Per-lane split-node state in shared memory, read by the lanes that help.
+struct SplitState {
+  u64* P;            // position of the split node
+  u64* O;
+  unsigned* pend;    // handed-out moves not yet reported
+  unsigned* acc;     // best helper result (pack_acc), 0 = none
+  unsigned* cut;     // 1 = the node was cut off or abandoned: helpers stop
+  int* lo;           // owner's best lower bound at the node (max(alpha, best))
+  int* beta;
+};
 
-__device__ __forceinline__ unsigned ld_volatile(const unsigned* p) {
+__device__ __forceinline__ unsigned ld_shared_volatile(const unsigned* p) {
   return *reinterpret_cast<const volatile unsigned*>(p);
 }
+__device__ __forceinline__ int ld_shared_volatile(const int* p) {
+  return *reinterpret_cast<const volatile int*>(p);
+}
+
+// k-th (0-based) set bit of m, m having more than k bits set.
+__device__ __forceinline__ int nth_bit(unsigned m, int k) {
+  for (int i = 0; i < k; ++i) m &= m - 1u;
+  return __ffs(static_cast<int>(m)) - 1;
+}
+
+// ---- rare paths, kept out of line so that the hot loop stays small ----
+
+// Table bounds of (P, O): 0 = not found, else 1 << 16 | (lower + 64) << 8 |
+// (upper + 64).
+__device__ __noinline__ unsigned tt_lookup(unsigned long long* tt, int bits, u64 P, u64 O) {
+  int lb, ub;
+  if (!tt_probe(tt, bits, tt_key(P, O), lb, ub)) return 0u;
+  return (1u << 16) | (static_cast<unsigned>(lb + 64) << 8) | static_cast<unsigned>(ub + 64);
+}
+
+// Stores the bound a closed node proves: best >= beta proves value >= best,
+// anything lower proves value <= best (an exact value is also an upper
+// bound).  Returns 1 if stored.
+__device__ __noinline__ int tt_record(unsigned long long* tt, int bits, u64 P, u64 O, int best,
+                                      int beta) {
+  const TTKey k = tt_key(P, O);
+  return best >= beta ? tt_store(tt, bits, k, best, 64) : tt_store(tt, bits, k, -64, best);
+}
+
+__device__ __noinline__ int stable_count(u64 O, u64 occ) { return popc(gpo_stable(O, occ)); }
+
+// A lane's split node: the shallowest of its open nodes (slots root_e down
+// to E + 1) with >= help_min empties that is not passed, has searched its
+// first move, has an open window and has a move left in its frame.  The
+// nodes' positions come from replaying the path from the root with the
+// stored flips.  Publishes the node in the split-node state and returns its
+// slot, or 0.
+__device__ __noinline__ int find_split_node(Frames fr, SplitState sp, int t, u64 X, u64 Y,
+                                            int root_e, int E, int help_min) {
+  for (int e = root_e; e > E; --e) {
+    u64 m, f;
+    unsigned meta;
+    fr.load(e, m, f, meta);
+    const int pas = meta_passed(meta);
+    if (pas) {
+      const u64 tmp = X;
+      X = Y;
+      Y = tmp;
+    }
+    const int b0 = meta_beta(meta), best0 = meta_best(meta), a0 = meta_alpha(meta);
+    const int lo0 = a0 > best0 ? a0 : best0;
+    const bool has = meta_list(meta) ? list_peek(m) != 0xFFF : m != 0;
+    if (e >= help_min && !pas && best0 > -65 && lo0 < b0 && has) {
+      sp.P[t] = X;
+      sp.O[t] = Y;
+      sp.lo[t] = lo0;
+      sp.beta[t] = b0;
+      sp.acc[t] = 0u;
+      sp.cut[t] = 0u;
+      sp.pend[t] = 0u;
+      return e;
+    }
+    const u64 ff = f & ~kResearch;
+    const u64 cx = Y ^ ff, cy = X ^ ff ^ (1ULL << meta_sq(meta));
+    X = cx;
+    Y = cy;
+  }
+  return 0;
+}
+
+}  // namespace
 
 __device__ __forceinline__ unsigned long long global_ns() {
 #ifdef GPO_SIMT_EMU  // the CPU emulation of this kernel used by the tests
@@ -110,133 +225,433 @@ __device__ __forceinline__ unsigned long long global_ns() {
 #endif
 }
 
-__device__ __forceinline__ unsigned pack_result(int v, int move) {
-  return (static_cast<unsigned>(v + 128) << 8) | static_cast<unsigned>(move & 255);
-}
+// Blocks per SM the register allocation must allow (128-thread blocks).
+#ifndef GPO_BATCHED_MIN_BLOCKS
+#define GPO_BATCHED_MIN_BLOCKS 1
+#endif
 
-__global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
+__global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BATCHED_MIN_BLOCKS)
+    batched_kernel(BatchedArgs args) {
   extern __shared__ __align__(16) u64 smem_raw[];
-  u64* const rays = smem_raw;           // 64 x 4 up-ray table (bitboard.cuh)
-  u64* const smem_u64 = smem_raw + 256;  // frame slots
+  const int B = blockDim.x;
+  const int t = threadIdx.x;
+  u64* const rays = smem_raw;  // 64 x 4 up-ray table (bitboard.cuh)
+  SplitState sp;
+  sp.P = smem_raw + 256;
+  sp.O = sp.P + B;
+  sp.pend = reinterpret_cast<unsigned*>(sp.O + B);
+  sp.acc = sp.pend + B;
+  sp.cut = sp.acc + B;
+  sp.lo = reinterpret_cast<int*>(sp.cut + B);
+  sp.beta = sp.lo + B;
+  u64* const fbase = reinterpret_cast<u64*>(sp.beta + B);  // B is a multiple of 32: aligned
   gpo_build_rays(rays);
+  sp.pend[t] = 0;
+  sp.acc[t] = 0;
+  sp.cut[t] = 0;
   __syncthreads();
-  Frames fr;
-  fr.B = blockDim.x;
-  fr.t = threadIdx.x;
-  fr.top = args.smem_top;
-  const int sslots = args.smem_top >= 2 ? args.smem_top - 1 : 0;
-  fr.sM = smem_u64;
-  fr.sF = smem_u64 + sslots * fr.B;
-  fr.sX = reinterpret_cast<unsigned*>(smem_u64 + 2 * sslots * fr.B);
-  fr.G = static_cast<size_t>(gridDim.x) * blockDim.x;
-  fr.gid = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int gslots = args.depth > args.smem_top ? args.depth - args.smem_top : 0;
-  fr.gM = reinterpret_cast<u64*>(args.gframes);
-  fr.gF = fr.gM + gslots * fr.G;
-  fr.gX = reinterpret_cast<unsigned*>(fr.gF + gslots * fr.G);
-  const size_t G = fr.G, gid = fr.gid;
 
-  const unsigned lane = threadIdx.x & 31;
+  Frames fr;
+  {
+    const bool shared = args.depth <= args.smem_top;
+    const long long slots = args.depth > 2 ? args.depth - 2 : 0;  // slots 3..depth
+    const long long threads = shared ? B : static_cast<long long>(gridDim.x) * B;
+    const long long me = shared ? t : static_cast<long long>(blockIdx.x) * B + t;
+    fr.m = shared ? fbase : reinterpret_cast<u64*>(args.gframes);
+    fr.f = fr.m + slots * threads;
+    fr.x = reinterpret_cast<unsigned*>(fr.f + slots * threads);
+    fr.stride = threads;
+    fr.off = me - 3 * threads;
+  }
+
+  const int lane = t & 31;
+  const int wbase = t - lane;  // thread index of lane 0 of this warp
   const unsigned lane_lt = (1u << lane) - 1u;
   const unsigned n = static_cast<unsigned>(args.n);
-  constexpr unsigned kNoMbox = 0xFFFFFFFFu;
-  unsigned long long total_nodes = 0, donations = 0, cancels = 0;
+  const int rpw = args.roots_per_warp > 0 ? args.roots_per_warp : 32;
+  unsigned long long total_nodes = 0, handouts = 0, stab_cuts = 0;
   unsigned long long tt_probes = 0, tt_hits = 0, tt_updates = 0;
-  bool tt_cut = false;  // the current node was closed by a table bound when created
 
-  // abort: close every open node of this lane's root at once (node budget
-  // exceeded, or the subtree was cancelled by its donor); an aborted
-  // subtree reports nothing but its completion.
-  bool busy = false, waiting = false, exhausted = false, started = false, abort = false;
-  unsigned pos = 0, task_mbox = kNoMbox, qidx = 0, chk = 0, dmask = 0;
-  int task_sq = 0;
-  // One deadline for the whole launch bounds every wait: a lane holding a
-  // ticket never gives it up early (a donor may still fill it), and when
-  // the deadline passes every lane unwinds and the call reports an error.
+  bool busy = false;    // a search is in progress in this lane
+  bool helper = false;  // ... and it is a move handed out by lane `towner`
+  bool abort = false;   // close every open node at once, reporting nothing
+  bool closed = false;  // the current node was closed when created (table or stability)
+  bool qdone = false;   // the input queue is used up (warp-uniform)
+  bool late = false;    // the launch deadline has passed (warp-uniform)
+  unsigned pos = 0;     // input position of the search (the owner's for a helper)
+  int towner = 0, tsq = 0, tlo = 0, tbeta = 0;
+  bool tres = false;    // a helper's move is being searched again
+  int spe = 0;          // slot of this lane's split node, 0 = none
+  unsigned chk = 0;
   const unsigned long long deadline = global_ns() + args.wait_limit_ns;
-  bool late = false;
   u64 P = 0, O = 0, moves = 0, lst = 0, P0 = 0, O0 = 0;
   int alpha = 0, beta = 0, best = 0, passed = 0, E = 0, root_e = 0, phase = PH_INIT;
   int rootbest = kMoveNoneDev;
   unsigned long long nodes = 0;
 
   for (;;) {
-    // ---- lanes without work: a queued subtree first (hard positions split
-    //      early must not wait behind the input queue) ----
-    if (!busy && !waiting && !exhausted && args.donate_min > 0) {
-      const unsigned h = ld_volatile(&args.stats->dq_head);
-      if (h < ld_volatile(&args.stats->dq_tail) && atomicCAS(&args.stats->dq_head, h, h + 1u) == h) {
-        qidx = h;
-        waiting = true;
+    __syncwarp();
+    ++chk;
+    if ((chk & 255u) == 0u) {
+      const bool over = global_ns() > deadline;
+      if (__any_sync(kFull, over)) {
+        if (!late && lane == 0) atomicOr(&args.stats->status, kErrWait);
+        late = true;
+        qdone = true;
       }
     }
-    // ---- then the input queue (one atomic per warp) ----
-    const unsigned need = __ballot_sync(0xffffffffu, !busy && !waiting && !exhausted);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned base = 0;
-      if (static_cast<int>(lane) == leader) base = atomicAdd(&args.stats->next, __popc(need));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (!busy && !waiting && !exhausted) {
-        const unsigned k = base + __popc(need & lane_lt);
-        if (k < n) {
-          const unsigned p = args.perm[k];
-          P = args.player[p];
-          O = args.opp[p];
-          E = 64 - popc(P | O);
-          if ((P & O) || E > args.depth) {  // rejected input: flagged, not searched
-            atomicOr(&args.stats->status, (P & O) ? kErrOverlap : kErrDepth);
-            args.score[p] = 0;
-            if (args.best) args.best[p] = kMoveNoneDev;
-            __threadfence();
-            atomicAdd(&args.stats->done, 1u);
-          } else {
-            busy = started = true;
-            pos = p;
-            task_mbox = kNoMbox;
-            alpha = args.root_alpha ? args.root_alpha[p] : -64;
-            beta = args.root_beta ? args.root_beta[p] : 64;
+    if (late && busy) abort = true;
+    // a helper whose split node was cut off abandons its subtree
+    if (busy && helper && !abort && ld_shared_volatile(&sp.cut[wbase + towner])) abort = true;
+
+    // ---- free lanes take input positions (at most rpw searches of its own
+    //      per warp; the rest of the warp helps) ----
+    const unsigned own = __ballot_sync(kFull, busy && !helper);
+    if (!qdone) {
+      const unsigned freem = __ballot_sync(kFull, !busy);
+      const int quota = rpw - __popc(own);
+      if (freem && quota > 0) {
+        unsigned takers = freem;
+        while (__popc(takers) > quota) takers &= ~(1u << (31 - __clz(static_cast<int>(takers))));
+        const int leader = __ffs(static_cast<int>(takers)) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&args.stats->next, static_cast<unsigned>(__popc(takers)));
+        base = __shfl_sync(kFull, base, leader);
+        if (base + static_cast<unsigned>(__popc(takers)) >= n) qdone = true;
+        if ((takers >> lane) & 1u) {
+          const unsigned k = base + static_cast<unsigned>(__popc(takers & lane_lt));
+          if (k < n) {
+            const unsigned p = args.perm[k];
+            P = args.player[p];
+            O = args.opp[p];
+            E = 64 - popc(P | O);
+            if ((P & O) || E > args.depth) {  // rejected input: flagged, not searched
+              atomicOr(&args.stats->status, (P & O) ? kErrOverlap : kErrDepth);
+              args.score[p] = 0;
+              if (args.best) args.best[p] = kMoveNoneDev;
+            } else {
+              busy = true;
+              helper = false;
+              pos = p;
+              alpha = -64;
+              beta = 64;
+              phase = PH_INIT;
+              root_e = E;
+              P0 = P;
+              O0 = O;
+              best = -65;
+              passed = 0;
+              nodes = 1;
+              rootbest = kMoveNoneDev;
+              abort = false;
+              closed = false;
+              tres = false;
+            }
           }
-        } else if (args.donate_min > 0) {
-          qidx = atomicAdd(&args.stats->dq_head, 1u);  // wait for a donated subtree
-          waiting = true;
-        } else {
-          exhausted = true;
         }
       }
     }
-    if (waiting) {
-      const unsigned qslot = qidx % args.task_cap;
-      if (ld_volatile(&args.ready[qslot]) == qidx + 1u) {
-        // The record was written by another SM: read it from L2 (.cg),
-        // never from a possibly stale L1 line.
-        __threadfence();
-        const DonatedTask* q = args.queue + qslot;
-        P = __ldcg(&q->player);
-        O = __ldcg(&q->opp);
-        const unsigned w = __ldcg(&q->window);
-        task_mbox = __ldcg(&q->mbox);
-        pos = __ldcg(&q->top);
-        __threadfence();
-        atomicExch(&args.consumed[qslot], qidx + 1u);  // the record may be refilled
-        E = 64 - popc(P | O);
-        alpha = static_cast<signed char>(w & 0xff);
-        beta = static_cast<signed char>((w >> 8) & 0xff);
-        task_sq = static_cast<int>((w >> 16) & 0xff);
-        waiting = false;
-        busy = started = true;
-      } else if (ld_volatile(&args.stats->done) >= n) {
-        waiting = false;
-        exhausted = true;
-      } else if (global_ns() > deadline) {
-        atomicOr(&args.stats->status, kErrWait);
-        waiting = false;
-        exhausted = true;
+
+    // ---- choose this lane's op; close finished nodes ----
+    int op = OP_NONE, sq = 0;
+    bool stall = false;
+    if (busy) {
+      if (phase != PH_INIT) {
+        for (;;) {
+          bool more;
+          if (phase == PH_KEY) more = true;
+          else if (phase == PH_LIST) more = list_peek(moves) != 0xFFF || (moves & kListOverflow);
+          else more = moves != 0;
+          const bool at_split = spe != 0 && spe == E;
+          if (at_split) {  // fold in what the helpers found
+            const unsigned a = ld_shared_volatile(&sp.acc[t]);
+            if (a) {
+              const int v = acc_value(a);
+              if (v > best) {
+                best = v;
+                if (E == root_e && !passed) rootbest = static_cast<int>(a & 255u);
+                if (v > alpha) alpha = v;
+              }
+            }
+          }
+          const bool fresh = best == -65;  // nothing searched yet
+          const bool finished = abort || alpha >= beta || (!more && !fresh);
+          if (!finished) {
+            if (at_split) {
+              const int lo = alpha > best ? alpha : best;
+              if (lo > ld_shared_volatile(&sp.lo[t])) sp.lo[t] = lo;
+            }
+            break;
+          }
+          if (at_split) {
+            if (ld_shared_volatile(&sp.pend[t]) != 0u) {  // helpers still out: wait for them
+              if (abort || alpha >= beta) sp.cut[t] = 1u;
+              stall = true;
+              break;
+            }
+            const unsigned a = ld_shared_volatile(&sp.acc[t]);  // their last reports
+            if (a && acc_value(a) > best) {
+              best = acc_value(a);
+              if (E == root_e && !passed) rootbest = static_cast<int>(a & 255u);
+            }
+            spe = 0;
+          }
+          // the node closes with value `best`
+          if (!closed && !abort && !passed && args.tt_min && E >= args.tt_min)
+            tt_updates += tt_record(args.tt, args.tt_bits, P, O, best, beta);
+          closed = false;
+          const int r = passed ? -best : best;
+          if (E == root_e) {
+            if (!helper) {  // the lane's own input position is solved
+              if (args.nodes_out) atomicAdd(&args.nodes_out[pos], nodes);
+              total_nodes += nodes;
+              args.score[pos] = static_cast<signed char>(abort ? 0 : r);
+              if (args.best) args.best[pos] = static_cast<signed char>(abort ? kMoveNoneDev : rootbest);
+              busy = false;
+              break;
+            }
+            const int v = -r;  // the value of the handed-out move for the split node
+            const int o = wbase + towner;
+            if (!abort && !tres && tlo + 1 < tbeta && v > tlo && v < tbeta &&
+                !ld_shared_volatile(&sp.cut[o])) {
+              // it beat the null window: search it again above what is known now
+              int lo_now = ld_shared_volatile(&sp.lo[o]);
+              const unsigned a = ld_shared_volatile(&sp.acc[o]);
+              if (a && acc_value(a) > lo_now) lo_now = acc_value(a);
+              const int a2 = v - 1 > lo_now ? v - 1 : lo_now;
+              if (a2 < tbeta) {
+                tres = true;
+                tlo = a2;
+                P = P0;
+                O = O0;
+                passed = 0;
+                alpha = -tbeta;
+                beta = -a2;
+                best = -65;
+                phase = PH_INIT;
+                ++nodes;
+                break;
+              }
+            }
+            if (!abort) {
+              const int exact = tres && v > tlo && v < tbeta;
+              atomicMax(&sp.acc[o], pack_acc(v, exact, tsq));
+            }
+            if (args.nodes_out) atomicAdd(&args.nodes_out[pos], nodes);
+            total_nodes += nodes;
+            atomicSub(&sp.pend[o], 1u);
+            busy = false;
+            helper = false;
+            break;
+          }
+          // back to the parent, unless this child must be searched again
+          u64 m, f;
+          unsigned meta;
+          fr.load(E + 1, m, f, meta);
+          const int pa = meta_alpha(meta), pb = meta_beta(meta), pbest = meta_best(meta);
+          const int v = -r;
+          const int plo = pa > pbest ? pa : pbest;
+          if (passed) {  // back to the orientation the node was created in
+            const u64 tmp = P;
+            P = O;
+            O = tmp;
+          }
+          if (!abort && !(f & kResearch) && pbest > -65 && plo + 1 < pb && v > plo && v < pb) {
+            // the child beat its null window: search it again with the
+            // window above its result (it is known to be worth at least v)
+            *fr.f_ptr(E + 1) = f | kResearch;
+            passed = 0;
+            alpha = -pb;
+            beta = 1 - v;
+            best = -65;
+            phase = PH_INIT;
+            ++nodes;
+            break;
+          }
+          ++E;
+          moves = m;
+          alpha = pa;
+          beta = pb;
+          best = pbest;
+          passed = meta_passed(meta);
+          phase = meta_list(meta) ? PH_LIST : PH_MASK;
+          const int psq = meta_sq(meta);
+          const u64 ff = f & ~kResearch;
+          const u64 pP = O ^ ff ^ (1ULL << psq), pO = P ^ ff;
+          P = pP;
+          O = pO;
+          if (v > best) {
+            best = v;
+            if (E == root_e && !passed) rootbest = psq;
+            if (v > alpha) alpha = v;
+          }
+        }
+      }
+      if (busy && !stall) {
+        if (phase == PH_INIT) {
+          op = OP_INIT;
+        } else if (phase == PH_KEY) {
+          const u64 b = moves & (0ULL - moves);
+          moves ^= b;
+          sq = ctz64(b);
+          op = OP_KEY;
+        } else if (phase == PH_LIST) {
+          const int e = list_peek(moves);
+          if (e != 0xFFF) {
+            sq = e & 63;
+            moves += 1ULL << 60;  // next list index
+            op = OP_MOVE;
+          } else {
+            op = OP_REMASK;
+          }
+        } else if (moves) {
+          const u64 b = pick_parity(moves, ~(P | O));
+          moves ^= b;
+          sq = ctz64(b);
+          op = OP_MOVE;
+        } else {
+          op = OP_PASS;  // no move and nothing searched: pass or game over
+        }
       }
     }
-    if (started) {  // a position or subtree was just taken: it is this lane's root
-      started = false;
-      phase = PH_INIT;
+
+    // ---- idle lanes take moves of split nodes of their warp ----
+    u64 hX = 0, hY = 0;
+    const unsigned freem = __ballot_sync(kFull, !busy);
+    const bool can_help = args.help_min > 0 && (qdone || __popc(own) >= rpw);
+    if (freem && can_help) {
+      // a busy lane without a split node looks for one now and then
+      if (busy && !stall && spe == 0 && !abort && (chk & 7u) == 0u && root_e >= args.help_min)
+        spe = find_split_node(fr, sp, t, P0, O0, root_e, E, args.help_min);
+      // offers: lanes below their split node with a move left in its frame
+      bool offer = false;
+      u64 om = 0;
+      unsigned ometa = 0;
+      int olo = 0, obeta = 0;
+      if (busy && !stall && !abort && spe != 0 && E < spe && !ld_shared_volatile(&sp.cut[t])) {
+        u64 f;
+        fr.load(spe, om, f, ometa);
+        olo = ld_shared_volatile(&sp.lo[t]);
+        const unsigned a = ld_shared_volatile(&sp.acc[t]);
+        if (a && acc_value(a) > olo) olo = acc_value(a);
+        obeta = sp.beta[t];
+        offer = olo < obeta && (meta_list(ometa) ? list_peek(om) != 0xFFF : om != 0);
+      }
+      const unsigned offm = __ballot_sync(kFull, offer);
+      if (offm) {
+        const int pairs = min(__popc(freem), __popc(offm));
+        int partner = lane, hsq = 0;
+        u64 sPv = 0, sOv = 0;
+        if (offer) {
+          const int k = __popc(offm & lane_lt);
+          if (k < pairs) {
+            partner = nth_bit(freem, k);
+            sPv = sp.P[t];
+            sOv = sp.O[t];
+            if (meta_list(ometa)) {
+              hsq = list_peek(om) & 63;
+              om += 1ULL << 60;
+            } else {
+              const u64 b = pick_parity(om, ~(sPv | sOv));
+              om ^= b;
+              hsq = ctz64(b);
+            }
+            *fr.m_ptr(spe) = om;
+            atomicAdd(&sp.pend[t], 1u);
+            ++handouts;
+          }
+        }
+        if (!busy) {
+          const int k = __popc(freem & lane_lt);
+          if (k < pairs) partner = nth_bit(offm, k);
+        }
+        const int g_sq = __shfl_sync(kFull, hsq, partner);
+        const int g_lo = __shfl_sync(kFull, olo, partner);
+        const int g_beta = __shfl_sync(kFull, obeta, partner);
+        const unsigned g_pos = __shfl_sync(kFull, pos, partner);
+        const u64 g_P = __shfl_sync(kFull, sPv, partner);
+        const u64 g_O = __shfl_sync(kFull, sOv, partner);
+        if (!busy && partner != lane) {
+          busy = true;
+          helper = true;
+          towner = partner;
+          tsq = g_sq;
+          tlo = g_lo;
+          tbeta = g_beta;
+          tres = false;
+          pos = g_pos;
+          hX = g_P;
+          hY = g_O;
+          sq = g_sq;
+          op = OP_HAND;
+        }
+      }
+    }
+
+    if (qdone && !__any_sync(kFull, busy)) break;
+    if (!__any_sync(kFull, op != OP_NONE)) {
+      __nanosleep(100);  // every busy lane is waiting for helpers
+      continue;
+    }
+
+    // ---- the uniform heavy step: one flip, then a mobility or flips ----
+    const bool play = op == OP_MOVE || op == OP_KEY || op == OP_HAND;
+    const bool same = op == OP_INIT || op == OP_REMASK;
+    const bool fold = op == OP_MOVE && E == 2;   // child has one empty: score it now
+    const bool last = op == OP_MOVE && E == 1;   // the move fills the board
+    const bool needmob = op != OP_NONE && !fold && !last;
+    const u64 X = op == OP_HAND ? hX : P;
+    const u64 Y = op == OP_HAND ? hY : O;
+    const u64 bit = play ? (1ULL << sq) : 0ULL;
+    // One flip site for up to three flips: the move; then, at a node with
+    // two empties, the child's last square s for the child, and for its
+    // opponent if the child cannot play it.
+    u64 f = 0, cP = X, cO = Y, fa = X, fb = Y;
+    int fs = sq, s1 = 0, n1 = 0;
+    bool fon = play;
+#pragma unroll 1
+    for (int k = 0;; ++k) {
+      // fs & 63: a lane that skips this flip may hold no square (-1)
+      const u64 r = fon ? gpo_flip(fa, fb, fs & 63, rays) : 0ULL;
+      if (k == 0) {
+        f = r;
+        cP = same ? X : (Y ^ f);
+        cO = same ? Y : (X ^ f ^ bit);
+        fa = cP;
+        fb = cO;
+        fs = ctz64(~(cP | cO));
+        fon = fold;
+      } else if (k == 1) {
+        n1 = popc(r);
+        fa = cO;
+        fb = cP;
+        fon = fold && n1 == 0;
+      } else {
+        // the child (cP to move) plays s if it can, else cO does, else the
+        // game ends with s empty
+        const int n2 = popc(r);
+        s1 = n1 ? 2 * (popc(cP) + n1 + 1) - 64
+                : (n2 ? 64 - 2 * (popc(cO) + n2 + 1) : gpo_final(cP, cO));
+        break;
+      }
+      if (!__any_sync(kFull, fon)) {
+        if (k == 1 && fold) s1 = 2 * (popc(cP) + n1 + 1) - 64;  // n1 > 0 here
+        break;
+      }
+    }
+    u64 cm = 0;
+    if (__any_sync(kFull, needmob)) cm = gpo_mobility(cP, cO);
+
+    // ---- bookkeeping on the result ----
+    // A node enters the keying phase (fastest-first) when it has two or more
+    // moves and at least args.ff empties: `moves` then holds the squares
+    // still to key and `lst` the list being built; the list replaces
+    // `moves` when done.
+    bool start_keys = false, created = false;
+    if (op == OP_HAND) {  // a helper's root: the handed-out move's child
+      P = cP;
+      O = cO;
+      E = 64 - popc(cP | cO);
       root_e = E;
       P0 = P;
       O0 = O;
@@ -244,274 +659,14 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
       passed = 0;
       nodes = 1;
       rootbest = kMoveNoneDev;
-      dmask = 0;
       abort = false;
-    }
-    if (__ballot_sync(0xffffffffu, !exhausted) == 0) break;
-
-    // ---- choose this lane's op; return finished nodes to their parents ----
-    int op = OP_NONE, sq = 0;
-    u64 DX = 0, DY = 0;
-    unsigned dq = 0, dwin = 0, dmbox = 0;
-    if (busy) {
-      if (phase == PH_INIT) {
-        op = OP_INIT;
-      } else {
-        bool stall = false;
-        for (;;) {
-          bool more;
-          if (phase == PH_KEY) more = true;
-          else if (phase == PH_LIST) more = list_peek(moves) != 0xFFF || (moves & kListOverflow);
-          else more = moves != 0;
-          const bool fresh = best == -65;  // nothing searched yet
-          const bool finished = abort || alpha >= beta || (!more && !fresh);
-          if (!finished) break;
-          if ((dmask >> E) & 1u) {
-            // moves handed to other lanes must report before the node closes;
-            // after a cutoff (or an abort) their results no longer matter
-            const size_t mb = static_cast<size_t>(E) * G + gid;
-            if (ld_volatile(&args.mbox_pend[mb]) != 0u) {
-              bool cut = abort || alpha >= beta;
-              if (!cut) {
-                const unsigned a = ld_volatile(&args.mbox_acc[mb]);
-                cut = a && static_cast<int>(a >> 8) - 128 >= beta;
-              }
-              if (cut && !ld_volatile(&args.mbox_cancel[mb])) {
-                atomicExch(&args.mbox_cancel[mb], 1u);
-                ++cancels;
-              }
-              if (!late && global_ns() <= deadline) {
-                stall = true;
-                break;
-              }
-              late = true;
-              atomicOr(&args.stats->status, kErrWait);
-            }
-            __threadfence();
-            const unsigned a = atomicAdd(&args.mbox_acc[mb], 0u);
-            if (a) {
-              const int v = static_cast<int>(a >> 8) - 128;
-              if (v > best) {
-                best = v;
-                if (E == root_e && !passed) rootbest = static_cast<int>(a & 255u);
-                if (v > alpha) alpha = v;
-              }
-            }
-            dmask &= ~(1u << E);
-          }
-          if (tt_cut) {
-            tt_cut = false;
-          } else if (args.tt_min && E >= args.tt_min && !passed && !abort) {
-            // best >= beta proves value >= best; anything lower proves
-            // value <= best (an exact value is also an upper bound)
-            const TTKey k = tt_key(P, O);
-            const bool ok = best >= beta ? tt_store(args.tt, args.tt_bits, k, best, 64)
-                                         : tt_store(args.tt, args.tt_bits, k, -64, best);
-            tt_updates += ok;
-          }
-          const int r = passed ? -best : best;
-          if (E == root_e) {  // the lane's root is done
-            if (args.nodes_out) atomicAdd(&args.nodes_out[pos], nodes);
-            total_nodes += nodes;
-            if (task_mbox == kNoMbox) {
-              args.score[pos] = static_cast<signed char>(abort ? (args.budget_mark ? -128 : 0) : r);
-              if (args.best) args.best[pos] = static_cast<signed char>(rootbest);
-              __threadfence();
-              atomicAdd(&args.stats->done, 1u);
-            } else {
-              if (!abort) atomicMax(&args.mbox_acc[task_mbox], pack_result(-r, task_sq));
-              __threadfence();
-              atomicSub(&args.mbox_pend[task_mbox], 1u);
-              atomicSub(&args.pos_tasks[pos], 1u);
-            }
-            busy = false;
-            break;
-          }
-          if (passed) {  // back to the orientation the node was created in
-            const u64 tmp = P;
-            P = O;
-            O = tmp;
-          }
-          ++E;
-          u64 f;
-          unsigned meta;
-          fr.load(E, moves, f, meta);
-          const int psq = static_cast<int>(meta & 63u);
-          alpha = static_cast<signed char>((meta >> 6) & 0xff);
-          beta = static_cast<signed char>((meta >> 14) & 0xff);
-          best = static_cast<signed char>((meta >> 22) & 0xff);
-          passed = static_cast<int>((meta >> 30) & 1u);
-          phase = (meta >> 31) ? PH_LIST : PH_MASK;
-          const u64 bit = 1ULL << psq;
-          const u64 pP = O ^ f ^ bit, pO = P ^ f;
-          P = pP;
-          O = pO;
-          const int v = -r;
-          if (v > best) {
-            best = v;
-            if (E == root_e && !passed) rootbest = psq;
-            if (v > alpha) alpha = v;
-          }
-        }
-        // ---- a handed-out subtree whose donor was cut off stops early ----
-        ++chk;
-        if (busy && !abort && task_mbox != kNoMbox && (chk & 15u) == 0u &&
-            ld_volatile(&args.mbox_cancel[task_mbox]))
-          abort = true;
-        if (busy && !abort && (chk & 255u) == 0u && global_ns() > deadline) {
-          atomicOr(&args.stats->status, kErrWait);
-          late = abort = true;
-        }
-        // ---- donation: hand a move of an ancestor to a waiting lane ----
-        if (busy && !stall && !abort && E < root_e && args.donate_min > 0 &&
-            root_e >= args.donate_min && (chk & 15u) == 8u) {
-          const unsigned t = ld_volatile(&args.stats->dq_tail);
-          const unsigned h = ld_volatile(&args.stats->dq_head);
-          // Hand out a move when a lane waits for one (ticket t is held), or
-          // when this root has run long (a hard position: split it while
-          // the rest of the batch still keeps the GPU busy) and few records
-          // are queued; record t % cap must have been read by the holder of
-          // ticket t - cap.
-          const bool asked = t < h;
-          const bool pushed = !asked && nodes > args.long_nodes && t - h < 1024u;
-          if ((asked || pushed) && ld_volatile(&args.pos_tasks[pos]) < args.max_tasks &&
-              (t < args.task_cap ||
-               ld_volatile(&args.consumed[t % args.task_cap]) == t - args.task_cap + 1u)) {
-            // Walk the path from the root (replaying the stored flips) to the
-            // shallowest node whose first move has returned and that has an
-            // untried move.
-            u64 X = P0, Y = O0;
-            int de = -1;
-            u64 dm = 0, df = 0;
-            unsigned dmeta = 0;
-            int dlo = 0, db = 0;
-            for (int e = root_e; e > E; --e) {
-              u64 m, f;
-              unsigned meta;
-              fr.load(e, m, f, meta);
-              const int pas = static_cast<int>((meta >> 30) & 1u);
-              if (pas) {
-                const u64 tmp = X;
-                X = Y;
-                Y = tmp;
-              }
-              const int b0 = static_cast<signed char>((meta >> 14) & 0xff);
-              const int best0 = static_cast<signed char>((meta >> 22) & 0xff);
-              if (e >= args.donate_min && !pas && best0 > -65) {
-                const int a0 = static_cast<signed char>((meta >> 6) & 0xff);
-                int lo0 = a0 > best0 ? a0 : best0;
-                if ((dmask >> e) & 1u) {
-                  const unsigned a = ld_volatile(&args.mbox_acc[static_cast<size_t>(e) * G + gid]);
-                  if (a && static_cast<int>(a >> 8) - 128 > lo0) lo0 = static_cast<int>(a >> 8) - 128;
-                }
-                if (lo0 < b0) {
-                  if (meta >> 31) {
-                    const int en = list_peek(m);
-                    if (en != 0xFFF) {
-                      sq = en & 63;
-                      dm = m + (1ULL << 60);
-                      de = e;
-                    }
-                  } else if (m) {
-                    const u64 b = pick_parity(m, ~(X | Y));
-                    sq = ctz64(b);
-                    dm = m ^ b;
-                    de = e;
-                  }
-                  if (de >= 0) {
-                    df = f;
-                    dmeta = meta;
-                    dlo = lo0;
-                    db = b0;
-                    break;
-                  }
-                }
-              }
-              const u64 bit = 1ULL << (meta & 63u);
-              const u64 cx = Y ^ f, cy = X ^ f ^ bit;
-              X = cx;
-              Y = cy;
-            }
-            if (de >= 0 && atomicCAS(&args.stats->dq_tail, t, t + 1u) == t) {
-              fr.store(de, dm, df, dmeta);
-              const size_t mb = static_cast<size_t>(de) * G + gid;
-              if (!((dmask >> de) & 1u)) {
-                atomicExch(&args.mbox_acc[mb], 0u);
-                atomicExch(&args.mbox_pend[mb], 0u);
-                atomicExch(&args.mbox_cancel[mb], 0u);
-                dmask |= 1u << de;
-              }
-              atomicAdd(&args.mbox_pend[mb], 1u);
-              atomicAdd(&args.pos_tasks[pos], 1u);
-              op = OP_DONATE;
-              DX = X;
-              DY = Y;
-              dq = t;
-              dmbox = static_cast<unsigned>(mb);
-              dwin = static_cast<unsigned>((-db) & 0xff) | (static_cast<unsigned>((-dlo) & 0xff) << 8) |
-                     (static_cast<unsigned>(sq) << 16);
-            }
-          }
-        }
-        if (busy && !stall && op == OP_NONE) {
-          if (phase == PH_KEY) {
-            const u64 b = moves & (0ULL - moves);
-            moves ^= b;
-            sq = ctz64(b);
-            op = OP_KEY;
-          } else if (phase == PH_LIST) {
-            const int e = list_peek(moves);
-            if (e != 0xFFF) {
-              sq = e & 63;
-              moves += 1ULL << 60;  // next list index
-              op = OP_MOVE;
-            } else {
-              op = OP_REMASK;
-            }
-          } else if (moves) {
-            const u64 b = pick_parity(moves, ~(P | O));
-            moves ^= b;
-            sq = ctz64(b);
-            op = OP_MOVE;
-          } else {
-            op = OP_PASS;  // no move and nothing searched: pass or game over
-          }
-        }
-      }
-    }
-    if (!__any_sync(0xffffffffu, op != OP_NONE)) {
-      __nanosleep(200);  // idle or waiting warp: leave issue slots to busy warps
-      continue;
-    }
-
-    // ---- the uniform heavy step: one flip, one mobility ----
-    const bool play = op == OP_MOVE || op == OP_KEY || op == OP_DONATE;
-    const bool same = op == OP_INIT || op == OP_REMASK;
-    const u64 X = op == OP_DONATE ? DX : P;
-    const u64 Y = op == OP_DONATE ? DY : O;
-    const u64 bit = play ? (1ULL << sq) : 0ULL;
-    const u64 f = play ? gpo_flip(X, Y, sq, rays) : 0ULL;
-    const u64 cP = same ? X : (Y ^ f);
-    const u64 cO = same ? Y : (X ^ f ^ bit);
-    const u64 cm = gpo_mobility(cP, cO);
-
-    // ---- bookkeeping on the result ----
-    // A node enters the keying phase (fastest-first) when it has moves and
-    // at least args.ff empties: `moves` then holds the squares still to key
-    // and `lst` the list being built; the list replaces `moves` when done.
-    bool start_keys = false;
-    if (op == OP_DONATE) {
-      const unsigned qslot = dq % args.task_cap;
-      DonatedTask* q = args.queue + qslot;
-      q->player = cP;
-      q->opp = cO;
-      q->window = dwin;
-      q->mbox = dmbox;
-      q->top = pos;
-      q->pad = 0;
-      __threadfence();
-      atomicExch(&args.ready[qslot], dq + 1u);
-      ++donations;
+      closed = false;
+      alpha = -(tlo + 1);  // null window above the split node's bound
+      beta = -tlo;
+      moves = cm;
+      phase = PH_MASK;
+      start_keys = (cm & (cm - 1)) && E >= args.ff;
+      created = true;
     } else if (op == OP_KEY) {
       int k = popc(cm) * 2 + ((bit & kCorners) ? 0 : 1);
       if (k > 62) k = 62;
@@ -523,8 +678,9 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
     } else if (op == OP_INIT) {
       moves = cm;
       phase = PH_MASK;
-      start_keys = cm && E >= args.ff;
-      if (cm && args.root_lists && task_mbox == kNoMbox && E >= args.learned_min) {
+      start_keys = (cm & (cm - 1)) && E >= args.ff;
+      if (cm && !helper && E == root_e && best == -65 && args.root_lists &&
+          E >= args.learned_min) {
         moves = args.root_lists[pos];  // the learned orderer's five best moves
         phase = PH_LIST;
         start_keys = false;
@@ -547,56 +703,71 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
         passed = 1;
         moves = cm;
         phase = PH_MASK;
-        start_keys = E >= args.ff;
+        start_keys = (cm & (cm - 1)) && E >= args.ff;
         if (E == root_e) rootbest = kMovePassDev;
       }
     } else if (op == OP_MOVE) {
       ++nodes;
-      const int lo = alpha > best ? alpha : best;
-      if (E == 1) {  // the move fills the board
-        const int v = -gpo_final(cP, cO);
+      if (last || fold) {
+        const int v = last ? -gpo_final(cP, cO) : -s1;
         if (v > best) {
           best = v;
           if (E == root_e && !passed) rootbest = sq;
           if (v > alpha) alpha = v;
         }
       } else {
+        const int lo = alpha > best ? alpha : best;
         fr.store(E, moves, f, pack_meta(sq, alpha, beta, best, passed, phase == PH_LIST));
+        // first move: the node's window; later moves: a null window above lo
+        const int na = (best > -65 && lo + 1 < beta) ? -(lo + 1) : -beta;
         --E;
         P = cP;
         O = cO;
-        alpha = -beta;
+        alpha = na;
         beta = -lo;
         best = -65;
         passed = 0;
         moves = cm;
         phase = PH_MASK;
-        start_keys = cm && E >= args.ff;
-        if (args.tt_min && E >= args.tt_min && !abort) {
-          int lb, ub;
-          ++tt_probes;
-          if (tt_probe(args.tt, args.tt_bits, tt_key(P, O), lb, ub)) {
-            ++tt_hits;
-            // a bound outside the window closes the node at once; one
-            // inside narrows it (sound for fail-soft search)
-            if (lb >= beta || ub <= alpha || lb >= ub) {
-              best = lb >= beta ? lb : (ub <= alpha ? ub : lb);
-              alpha = beta;
-              tt_cut = true;
-              start_keys = false;
-            } else {
-              if (lb > alpha) alpha = lb;
-              if (ub < beta) beta = ub;
-            }
+        start_keys = (cm & (cm - 1)) && E >= args.ff;
+        created = true;
+      }
+    }
+    if (created && !abort) {
+      if (args.tt_min && E >= args.tt_min) {
+        ++tt_probes;
+        const unsigned h = tt_lookup(args.tt, args.tt_bits, P, O);
+        if (h) {
+          ++tt_hits;
+          const int lb = static_cast<int>((h >> 8) & 0xff) - 64, ub = static_cast<int>(h & 0xff) - 64;
+          // a bound outside the window closes the node at once; one
+          // inside narrows it (sound for fail-soft search)
+          if (lb >= beta || ub <= alpha || lb >= ub) {
+            best = lb >= beta ? lb : (ub <= alpha ? ub : lb);
+            alpha = beta;
+            closed = true;
+            start_keys = false;
+          } else {
+            if (lb > alpha) alpha = lb;
+            if (ub < beta) beta = ub;
           }
         }
-        if (args.node_budget && nodes > args.node_budget && !abort) {
-          // watchdog: every open node of this lane closes at once (still
-          // collecting any handed-out moves); the call reports the error,
-          // or, in a first pass, the position is marked for the second
-          if (!args.budget_mark) atomicOr(&args.stats->status, kErrBudget);
-          abort = true;
+      }
+      if (!closed && args.stab_min && E >= args.stab_min && alpha >= args.stab_gate) {
+        const int cap = 64 - 2 * stable_count(O, P | O);
+        if (cap <= alpha) {  // the side to move cannot reach alpha
+          best = cap;
+          alpha = beta;
+          closed = true;
+          start_keys = false;
+          ++stab_cuts;
         }
+      }
+      if (args.node_budget && nodes > args.node_budget && !helper) {
+        // watchdog: every open node of this lane closes at once; the call
+        // reports the error
+        atomicOr(&args.stats->status, kErrBudget);
+        abort = true;
       }
     }
     if (start_keys) {
@@ -605,16 +776,20 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchedArgs args) {
     }
   }
   warp_add(&args.stats->nodes, total_nodes);
-  warp_add(&args.stats->donations, donations);
-  warp_add(&args.stats->cancels, cancels);
+  warp_add(&args.stats->handouts, handouts);
+  warp_add(&args.stats->stab_cuts, stab_cuts);
   warp_add(&args.stats->tt_probes, tt_probes);
   warp_add(&args.stats->tt_hits, tt_hits);
   warp_add(&args.stats->tt_updates, tt_updates);
 }
 
+size_t batched_smem_bytes(int threads, int smem_top) {
+  const int sslots = smem_top >= 3 ? smem_top - 2 : 0;
+  return kRayBytes + static_cast<size_t>(threads) * (kSplitBytes + sslots * kFrameBytes);
+}
+
 cudaError_t batched_grid(int threads, int smem_top, int sms, int* grid, size_t* smem) {
-  const int sslots = smem_top >= 2 ? smem_top - 1 : 0;
-  *smem = kRayBytes + static_cast<size_t>(threads) * sslots * kFrameBytes;
+  *smem = batched_smem_bytes(threads, smem_top);
   cudaError_t e = cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(*smem));
   if (e != cudaSuccess) return e;
@@ -627,8 +802,8 @@ cudaError_t batched_grid(int threads, int smem_top, int sms, int* grid, size_t* 
 }
 
 cudaError_t batched_plan(int threads, int depth, int* smem_top) {
-  // Blocks per SM that registers allow, then as many shared-memory frame
-  // slots as fit beside them without lowering that count.
+  // Blocks per SM that registers allow; the frames go to shared memory when
+  // all depth - 2 slots fit beside that many blocks, else to global memory.
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel, threads, 0);
   if (e != cudaSuccess) return e;
@@ -638,13 +813,17 @@ cudaError_t batched_plan(int threads, int depth, int* smem_top) {
     e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  const int per_block = smem_sm / per_sm - 1024 - kRayBytes;  // 1 KB per block is reserved
-  const int slots = per_block > 0 ? per_block / (threads * kFrameBytes) : 0;
-  int top = slots + 1;
-  if (top > depth) top = depth;
-  if (top < 1) top = 1;
-  *smem_top = top;
+  // 1 KB per block is reserved by the hardware
+  const long per_block = static_cast<long>(smem_sm) / per_sm - 1024 - kRayBytes -
+                         static_cast<long>(threads) * kSplitBytes;
+  const long need = static_cast<long>(depth > 2 ? depth - 2 : 0) * threads * kFrameBytes;
+  *smem_top = need <= per_block ? depth : 2;
   return cudaSuccess;
+}
+
+size_t batched_gframe_bytes(int depth, int smem_top, size_t lanes) {
+  if (depth <= smem_top) return 0;
+  return static_cast<size_t>(depth > 2 ? depth - 2 : 0) * kFrameBytes * lanes;
 }
 
 cudaError_t launch_batched(const BatchedArgs& args, BatchedLaunch& cfg, int sms, cudaStream_t s) {
@@ -656,12 +835,11 @@ cudaError_t launch_batched(const BatchedArgs& args, BatchedLaunch& cfg, int sms,
   if (cfg.grid > 0 && cfg.grid < grid) grid = cfg.grid;
   cfg.grid = grid;
   cfg.smem = smem;
-  // Idle lanes wait (bounded) for subtrees donated by other blocks, so every
-  // block must be resident at once: a cooperative launch guarantees it.
-  BatchedArgs a = args;
-  void* kargs[] = {&a};
-  return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(batched_kernel), dim3(grid),
-                                     dim3(threads), kargs, smem, s);
+  // Lanes wait only for lanes of their own warp, so an ordinary launch
+  // suffices: warps leave as soon as the queue is used up and their lanes
+  // are idle.
+  batched_kernel<<<grid, threads, smem, s>>>(args);
+  return cudaGetLastError();
 }
 
 }  // namespace gpo

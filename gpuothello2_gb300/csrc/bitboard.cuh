@@ -102,6 +102,52 @@ __device__ __forceinline__ int gpo_final(u64 P, u64 O) {
   return pc == oc ? 0 : (pc > oc ? 64 - 2 * oc : 2 * pc - 64);
 }
 
+// ---- stable discs ----
+// A subset of the discs of `O` that no sequence of moves can flip: a disc is
+// kept when, along each of the four line directions, its line is full, it
+// sits on the board edge across that direction, or a neighbour along it is
+// already kept.  Such a disc cannot be flipped along that line (a flip needs
+// an empty square to play on and a bracketing disc on the far side, and the
+// kept neighbour would have to flip with it).  Sound after any number of
+// rounds, so the loop is bounded; it stops early when nothing is added.
+// The side to move can then score at most 64 - 2 * popc(result).
+__device__ __forceinline__ u64 gpo_stable(u64 O, u64 occ) {
+  constexpr u64 notA = 0xfefefefefefefefeULL, notH = 0x7f7f7f7f7f7f7f7fULL;
+  constexpr u64 notAB = 0xfcfcfcfcfcfcfcfcULL, notGH = 0x3f3f3f3f3f3f3f3fULL;
+  constexpr u64 notAD = 0xf0f0f0f0f0f0f0f0ULL, notEH = 0x0f0f0f0f0f0f0f0fULL;
+  constexpr u64 colAH = 0x8181818181818181ULL, row18 = 0xff000000000000ffULL;
+  constexpr u64 edge = colAH | row18;
+  // full rows: bit 8r survives the three folds only if the whole byte is set
+  u64 h = occ & (occ >> 1);
+  h &= h >> 2;
+  h &= h >> 4;
+  h = (h & 0x0101010101010101ULL) * 0xffULL;
+  // full columns: bit c of row 0 survives only if the whole column is set
+  u64 v = occ & (occ >> 8);
+  v &= v >> 16;
+  v &= v >> 32;
+  v = (v & 0xffULL) * 0x0101010101010101ULL;
+  // diagonals: spread the empty squares along each diagonal (1, 2, 4 steps);
+  // squares never reached lie on full diagonals
+  u64 e9 = ~occ, e7 = ~occ;
+  e9 |= ((e9 << 9) & notA) | ((e9 >> 9) & notH);
+  e9 |= ((e9 << 18) & notAB) | ((e9 >> 18) & notGH);
+  e9 |= ((e9 << 36) & notAD) | ((e9 >> 36) & notEH);
+  e7 |= ((e7 << 7) & notH) | ((e7 >> 7) & notA);
+  e7 |= ((e7 << 14) & notGH) | ((e7 >> 14) & notAB);
+  e7 |= ((e7 << 28) & notEH) | ((e7 >> 28) & notAD);
+  const u64 H = h | colAH, V = v | row18, D9 = ~e9 | edge, D7 = ~e7 | edge;
+  u64 st = 0;
+  for (int i = 0; i < 8; ++i) {
+    const u64 n = O & (H | ((st << 1) & notA) | ((st >> 1) & notH)) & (V | (st << 8) | (st >> 8)) &
+                  (D9 | ((st << 9) & notA) | ((st >> 9) & notH)) &
+                  (D7 | ((st << 7) & notH) | ((st >> 7) & notA));
+    if (n == st) break;
+    st = n;
+  }
+  return st;
+}
+
 // Score after the last empty square `sq` is filled (or passed on).  With one
 // empty the disc difference after a move follows from the flip count alone.
 __device__ __forceinline__ int gpo_solve1(u64 P, u64 O, int sq, const u64* rays) {

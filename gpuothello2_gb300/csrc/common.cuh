@@ -25,7 +25,7 @@ enum : unsigned int {
   kErrBudget = 1u << 2,    // a search hit the per-position node budget
   kErrTable = 1u << 3,     // a table update gave up after its retry limit
   kErrInternal = 1u << 4,  // stack index out of range (never expected)
-  kErrWait = 1u << 5,      // an idle lane waited longer than the wait limit
+  kErrWait = 1u << 5,      // the search launch ran past its deadline
 };
 
 // Per-launch device counters (one instance in device memory per context).
@@ -35,13 +35,10 @@ struct DeviceStats {
   unsigned long long tt_hits;
   unsigned long long tt_updates;
   unsigned long long learned_calls;
+  unsigned long long handouts;   // moves of split nodes searched by helper lanes
+  unsigned long long stab_cuts;  // nodes closed by the stability cutoff
   unsigned int status;
-  unsigned int next;         // work-queue cursor of the persistent kernel
-  unsigned int done;         // input positions finished
-  unsigned int dq_head;      // donation queue: records reserved by idle lanes
-  unsigned int dq_tail;      // donation queue: records claimed by donors
-  unsigned long long donations;
-  unsigned long long cancels;    // handed-out subtrees abandoned after a cutoff
+  unsigned int next;             // work-queue cursor of the persistent kernel
 };
 
 __device__ __forceinline__ int ctz64(u64 x) { return __ffsll(static_cast<long long>(x)) - 1; }

@@ -14,9 +14,11 @@
 //
 // Limits: at most GPO_NOALLOC_MAX_POSITIONS positions and depth at most
 // GPO_NOALLOC_MAX_DEPTH per call; larger calls are rejected with GPO_ERR_ARG
-// / GPO_ERR_DEPTH before any GPU work.  Subtree splitting and the
-// transposition table are off (they need per-call buffers); scores are the
-// same exact scores.
+// / GPO_ERR_DEPTH before any GPU work.  The transposition table is off (it
+// needs its own buffer); helping between the lanes of a warp needs no
+// buffer and stays on; scores are the same exact scores.  When the frame
+// slots do not fit in shared memory and would not fit the array for the
+// full grid, the launch uses fewer blocks (the largest grid that fits).
 //
 // The array is shared by every call and keeps the last call's contents: the
 // status word and bucket counters are cleared at the start of each call, and
@@ -47,7 +49,6 @@ constexpr size_t kFramesOff =
 constexpr size_t kFramesBytes = 8u << 20;  // frame slots above the shared-memory tier
 constexpr size_t kScratchBytes = kFramesOff + kFramesBytes;
 
-constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char* g_scratch_ptr[kMaxDevices] = {nullptr};
 
@@ -116,9 +117,12 @@ extern "C" int solve_batch_device_noalloc(const uint64_t* d_player, const uint64
   a.perm = perm;
   a.n = n;
   a.depth = depth;
-  a.ff = 9;
   a.score = reinterpret_cast<signed char*>(d_score);
   a.stats = stats;
+  a.ff = 6;
+  a.stab_min = 6;
+  a.stab_gate = 30;
+  a.help_min = 7;
   a.wait_limit_ns = 600000ULL * 1000000ULL;
   BatchedLaunch cfg;
   cfg.threads = 128;
@@ -127,13 +131,18 @@ extern "C" int solve_batch_device_noalloc(const uint64_t* d_player, const uint64
   size_t smem = 0;
   if (batched_grid(cfg.threads, a.smem_top, sms, &cfg.grid, &smem) != cudaSuccess)
     return GPO_ERR_CUDA;
-  const int gslots = depth > a.smem_top ? depth - a.smem_top : 0;
-  if (gslots > 0) {  // fewer lanes if the overflow slots would not fit
-    const size_t lanes = kFramesBytes / (static_cast<size_t>(gslots) * 20);
-    const int grid_cap = static_cast<int>(lanes / cfg.threads);
+  // Frame slots that do not fit in shared memory come from the fixed array:
+  // when they would not fit it for the full grid, the grid shrinks to the
+  // largest that fits.
+  const size_t per_block = batched_gframe_bytes(depth, a.smem_top, cfg.threads);
+  if (per_block > 0) {
+    const int grid_cap = static_cast<int>(kFramesBytes / per_block);
     if (grid_cap < 1) return GPO_ERR_DEPTH;
     if (cfg.grid > grid_cap) cfg.grid = grid_cap;
   }
+  const long warps = static_cast<long>(cfg.grid) * (cfg.threads / 32);
+  const long per = (n + warps - 1) / warps;
+  a.roots_per_warp = static_cast<int>(per < 1 ? 1 : (per > 32 ? 32 : per));
   a.gframes = base + kFramesOff;
   if (launch_batched(a, cfg, sms, s) != cudaSuccess) return GPO_ERR_CUDA;
 

@@ -55,48 +55,44 @@ extern "C" {
 
 typedef struct gpo_options {
   int method;                 /* GPO_METHOD_* */
-  int use_table;              /* transposition table: 1 on; 0 or -1 (auto) off; cleared at
+  int use_table;              /* transposition table: 0 off, 1 or -1 (auto) on; cleared at
                                  every call, so no result carries over */
   int use_learned;            /* learned root ordering (gpo_mlp_load): -1 auto (on when a
                                  network is loaded), 0 off, 1 on */
   int threads_per_block;      /* 32..256, multiple of 32; 0 = 128 */
-  int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties; 0 = tuned */
+  int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties;
+                                 0 = default (6) */
   int learned_min_empties;    /* learned ordering at roots with >= this many empties; 0 = 14 */
-  uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog) */
-  int split_min_empties;      /* hard positions: 0 = positions over expand_budget nodes are
-                                 replaced by their children, solved in further passes (up to
-                                 6 levels); > 0 = they are solved again with subtrees handed
-                                 to idle lanes from nodes with this many empties; negative =
-                                 one pass, no splitting */
-  int wait_limit_ms;          /* deadline of one search launch (a watchdog on waits between
-                                 lanes); 0 = 600000 */
-  int table_bits;             /* transposition table of 2^table_bits 16-byte entries; 0 = 24 */
-  int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 11 */
-  int smem_frames;            /* search frames kept in shared memory: 0 = as many as keep the
-                                 register-limited occupancy, > 0 = at most this many, negative
-                                 = none (every frame in the global frame array) */
-  uint64_t expand_budget;     /* split_min_empties == 0: per-position node budget of each
-                                 expansion level; 0 = 2^22 */
-  int expand_windows;         /* split_min_empties == 0: 0 = every child of a hard position
-                                 searched with a full window; 1 = principal variation
-                                 first: the first child in fastest-first order with a full
-                                 window, its siblings with a null window around the bound it
-                                 gives, and only the siblings that beat it searched again;
-                                 2 = the same at every expanded position, recursively, with
-                                 the siblings of a position cut off by its first child never
-                                 searched */
+  uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog: GPO_ERR_TIMEOUT) */
+  int help_min_empties;       /* idle lanes of a warp help its busy lanes with moves of nodes
+                                 that have >= this many empties (young brothers wait, after
+                                 the node's first move); 0 = default (7), negative = off */
+  int wait_limit_ms;          /* deadline of one search launch; 0 = 600000 */
+  int table_bits;             /* transposition table of 2^table_bits 16-byte entries
+                                 (16..32); 0 = 24 */
+  int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 7 */
+  int smem_frames;            /* search frames (depth - 2 slots per lane) in shared memory:
+                                 0 = when they all fit at the register-limited occupancy,
+                                 > 0 = only if at most this many are needed, negative = never
+                                 (every frame in the global frame array) */
+  int stability_min_empties;  /* stability cutoff at nodes with >= this many empties;
+                                 0 = default (6), negative = off */
+  int roots_per_warp;         /* input positions a warp searches at once, the rest of its
+                                 lanes helping (1..32); 0 = from the batch size: 32 when the
+                                 batch fills the GPU, fewer for small batches */
 } gpo_options;
 
 typedef struct gpo_stats {
-  uint64_t nodes;         /* positions visited (root, children, pass frames) */
-  uint64_t table_probes;  /* transposition-table lookups */
-  uint64_t table_hits;    /* lookups that found the position */
-  uint64_t table_updates; /* stores into the table */
-  uint64_t learned_calls; /* learned-orderer evaluations */
-  uint64_t splits;        /* subtrees handed to other lanes */
-  double kernel_ms;       /* device time of the search kernels (CUDA events) */
-  double total_ms;        /* wall time of the call */
-  uint64_t launches;      /* kernels the call launched */
+  uint64_t nodes;          /* positions visited (root, children, pass frames) */
+  uint64_t table_probes;   /* transposition-table lookups */
+  uint64_t table_hits;     /* lookups that found the position */
+  uint64_t table_updates;  /* stores into the table */
+  uint64_t learned_calls;  /* learned-orderer evaluations */
+  uint64_t splits;         /* moves of split nodes searched by helper lanes */
+  double kernel_ms;        /* device time of the search kernel (CUDA events) */
+  double total_ms;         /* wall time of the call */
+  uint64_t launches;       /* kernels the call launched */
+  uint64_t stability_cuts; /* nodes closed by the stability cutoff */
 } gpo_stats;
 
 /* Fills *opt with the defaults (all fields "auto"/0). */

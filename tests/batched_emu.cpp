@@ -4,17 +4,17 @@
 //
 // emu_batched() runs batched_kernel as one block of `warps` x 32 CPU threads
 // over n positions, with the buffers the C-ABI layer would give it: the
-// empties-descending queue order, the frame tiers, the donation mailboxes
-// and record ring, the transposition table and learned root lists.  Tests
-// compare its scores with the oracle and exercise the code paths a GPU run
-// takes (in-kernel donation across warps, the table, node budgets).
+// empties-descending queue order, the frame placements, the transposition
+// table and learned root lists.  Tests compare its scores with the oracle
+// and exercise the code paths a GPU run takes (helping between the lanes
+// of a warp, the table, the stability cutoff, node budgets).
 #include <algorithm>
 #include <memory>
 #include <numeric>
 #include <thread>
 #include <vector>
 
-#include "../gpuothello2_gb300/csrc/batched.cu"
+#include "batched_emu.cu"
 
 thread_local simt_uint3 threadIdx, blockIdx;
 simt_uint3 blockDim, gridDim;
@@ -23,9 +23,9 @@ SimtBarrier* simt_block = nullptr;
 std::mutex simt_cas128_mutex;
 
 namespace gpo {
-// dynamic shared memory of the one emulated block: the ray table and up to
-// 31 frame slots of 20 bytes for 128 threads
-constexpr size_t kEmuSmemWords = (kRayBytes + 128 * 31 * kFrameBytes) / 8 + 8;
+// dynamic shared memory of the one emulated block: the ray table, the
+// split-node state and up to 30 frame slots for 128 threads
+constexpr size_t kEmuSmemWords = (kRayBytes + 128 * (kSplitBytes + 30 * kFrameBytes)) / 8 + 8;
 alignas(16) u64 smem_raw[kEmuSmemWords];
 }  // namespace gpo
 
@@ -33,20 +33,20 @@ extern "C" {
 
 struct EmuOptions {
   int warps;                        // 1..4
-  int ff;                           // fastest-first threshold (0 = 9)
-  int smem_slots;                   // frame slots in shared memory (0 = none)
-  int donate_min;                   // in-kernel donation from nodes with this many empties (0 = off)
-  unsigned long long long_nodes;    // root size after which it hands out moves unasked
-  unsigned max_tasks;               // outstanding subtrees per position
+  int ff;                           // fastest-first threshold (0 = 6)
+  int shared_frames;                // 1: frame slots in shared memory, 0: in the global array
+  int help_min;                     // helping from nodes with this many empties (0 = off)
+  int roots_per_warp;               // input positions per warp (0 = 32)
+  int stab_min;                     // stability cutoff (0 = off)
+  int stab_gate;
   unsigned long long node_budget;   // per position, 0 = none
-  int budget_mark;                  // over budget: score -128 instead of an error
   int tt_bits;                      // 0 = no table
   int tt_min;
   const unsigned long long* root_lists;  // learned root orders per position, or null
   int learned_min;
 };
 
-// stats: nodes, table probes, hits, updates, donations, cancels, status
+// stats: nodes, table probes, hits, updates, handouts, stability cuts, status
 int emu_batched(const unsigned long long* P, const unsigned long long* O, int n, int depth,
                 const EmuOptions* opt, signed char* score, signed char* best,
                 unsigned long long* nodes, unsigned long long* stats) {
@@ -65,50 +65,31 @@ int emu_batched(const unsigned long long* P, const unsigned long long* O, int n,
   a.perm = perm.data();
   a.n = n;
   a.depth = depth;
-  a.ff = opt->ff > 0 ? opt->ff : 9;
+  a.ff = opt->ff > 0 ? opt->ff : 6;
   a.score = score;
   a.best = best;
   a.nodes_out = nodes;
   DeviceStats st = {};
   a.stats = &st;
   a.node_budget = opt->node_budget;
-  a.budget_mark = opt->budget_mark;
-  int top = opt->smem_slots > 0 ? opt->smem_slots + 1 : 1;
-  if (top > depth) top = depth;
-  if (top > 32) top = 32;
-  a.smem_top = top;
-  const size_t gslots = static_cast<size_t>(depth > top ? depth - top : 0);
-  std::vector<u64> gframes((gslots * kFrameBytes * T) / 8 + 1);
+  a.help_min = opt->help_min;
+  a.roots_per_warp = opt->roots_per_warp > 0 ? opt->roots_per_warp : 32;
+  a.stab_min = opt->stab_min;
+  a.stab_gate = opt->stab_gate;
+  a.smem_top = opt->shared_frames ? depth : 2;
+  std::vector<u64> gframes(batched_gframe_bytes(depth, a.smem_top, static_cast<size_t>(T)) / 8 + 1);
   a.gframes = reinterpret_cast<unsigned char*>(gframes.data());
-  const size_t mboxes = static_cast<size_t>(kMaxEmpties + 1) * T;
-  std::vector<unsigned> acc(mboxes), pend(mboxes), cancel(mboxes), pos_tasks(n + 1);
-  const unsigned task_cap = 4096;
-  std::vector<DonatedTask> queue(task_cap);
-  std::vector<unsigned> ready(task_cap), consumed(task_cap);
-  if (opt->donate_min > 0) {
-    a.donate_min = opt->donate_min;
-    a.long_nodes = opt->long_nodes ? opt->long_nodes : (1ULL << 21);
-    a.pos_tasks = pos_tasks.data();
-    a.max_tasks = opt->max_tasks ? opt->max_tasks : 32;
-    a.task_cap = task_cap;
-    a.mbox_acc = acc.data();
-    a.mbox_pend = pend.data();
-    a.mbox_cancel = cancel.data();
-    a.queue = queue.data();
-    a.ready = ready.data();
-    a.consumed = consumed.data();
-  }
   std::vector<u64> table;
   if (opt->tt_bits > 0) {
     table.assign(static_cast<size_t>(2) << opt->tt_bits, 0);
     a.tt = table.data();
     a.tt_bits = opt->tt_bits;
-    a.tt_min = opt->tt_min > 0 ? opt->tt_min : 11;
+    a.tt_min = opt->tt_min > 0 ? opt->tt_min : 7;
   }
   a.root_lists = opt->root_lists;
   a.learned_min = opt->learned_min > 0 ? opt->learned_min : 14;
   a.wait_limit_ns = 600ULL * 1000000000ULL;
-  const size_t smem = kRayBytes + static_cast<size_t>(T) * (top >= 2 ? top - 1 : 0) * kFrameBytes;
+  const size_t smem = batched_smem_bytes(T, a.smem_top);
   if (smem > sizeof(smem_raw)) return -1;
 
   blockDim = {static_cast<unsigned>(T), 1, 1};
@@ -135,8 +116,8 @@ int emu_batched(const unsigned long long* P, const unsigned long long* O, int n,
   stats[1] = st.tt_probes;
   stats[2] = st.tt_hits;
   stats[3] = st.tt_updates;
-  stats[4] = st.donations;
-  stats[5] = st.cancels;
+  stats[4] = st.handouts;
+  stats[5] = st.stab_cuts;
   stats[6] = st.status;
   return 0;
 }

@@ -1,6 +1,6 @@
 // The whole solve pipeline of the library -- the C-ABI layer (capi.cu), the
-// preparation, expansion and combination kernels (prep.cu), the plain and
-// batched search kernels and the allocation-free entry point -- compiled as
+// bucketing and generator kernels (prep.cu), the plain and batched search
+// kernels and the allocation-free entry point -- compiled as
 // host C++ and run on CPU threads under the SIMT emulation
 // (tests/simt/simt_prelude.h, tests/simt/cuda_runtime.h).  Test
 // infrastructure only: the product never links this file, and the library
@@ -9,16 +9,15 @@
 // exports and checks it against the golden scores and the oracle without a
 // GPU.
 //
-// The emulation build copies prep.cu and plain.cu with their
+// The emulation build copies batched.cu, prep.cu and plain.cu with their
 // `k<<<grid, block, smem, stream>>>(args)` launches rewritten to
 // simt_launch(k, simt_cfg(grid, block, smem, stream), args) (see
-// gpuothello2_gb300/build.py); batched.cu, noalloc.cu and capi.cu compile
-// unchanged.  The learned orderer (mlp.cu, tensor-core code) is left out:
+// gpuothello2_gb300/build.py); noalloc.cu and capi.cu compile unchanged.  The learned orderer (mlp.cu, tensor-core code) is left out:
 // the solver sees no network loaded.
 
 // batched.cu's dynamic shared memory is `extern __shared__`: keep
 // __shared__ empty for it ...
-#include "../gpuothello2_gb300/csrc/batched.cu"
+#include "batched_emu.cu"
 
 // ... and make the other kernels' static __shared__ arrays function
 // statics: blocks of an ordinary launch run one after another.
@@ -37,8 +36,10 @@ std::mutex simt_cas128_mutex;
 
 namespace gpo {
 
-// dynamic shared memory of the one emulated block of the batched kernel
-constexpr size_t kEmuSmemWords = (kRayBytes + 256 * 31 * kFrameBytes) / 8 + 8;
+// dynamic shared memory of a block of the batched kernel (blocks of a launch
+// run one after another): the ray table, the split-node state and up to 30
+// frame slots for 256 threads
+constexpr size_t kEmuSmemWords = (kRayBytes + 256 * (kSplitBytes + 30 * kFrameBytes)) / 8 + 8;
 alignas(16) u64 smem_raw[kEmuSmemWords];
 
 // the learned orderer is not part of this build
@@ -49,26 +50,4 @@ int mlp_order_roots(const u64*, const u64*, const unsigned*, long, u64*, cudaStr
   return GPO_ERR_ARG;
 }
 
-namespace {
-
-// The cooperative launch of batched_kernel: every block at once (their
-// lanes may wait on one another), each with its own threads.
-cudaError_t emu_cooperative(const void* f, dim3 grid, dim3 block, void** args) {
-  if (f != reinterpret_cast<const void*>(batched_kernel) || grid.x != 1) return 1;
-  const size_t smem = kRayBytes + static_cast<size_t>(block.x) *
-                                      (static_cast<const BatchedArgs*>(args[0])->smem_top >= 2
-                                           ? static_cast<const BatchedArgs*>(args[0])->smem_top - 1
-                                           : 0) *
-                                      kFrameBytes;
-  if (smem > sizeof(smem_raw)) return cudaErrorInvalidConfiguration;
-  const BatchedArgs a = *static_cast<const BatchedArgs*>(args[0]);
-  simt_run_block(0, 1, block.x, [&] { batched_kernel(a); });
-  return cudaSuccess;
-}
-
-struct HookInstaller {
-  HookInstaller() { simt_coop_hook() = emu_cooperative; }
-} g_install_hook;
-
-}  // namespace
 }  // namespace gpo

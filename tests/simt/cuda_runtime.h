@@ -116,6 +116,7 @@ inline cudaError_t cudaGetDevice(int* d) {
   *d = 0;
   return cudaSuccess;
 }
+inline cudaError_t cudaSetDevice(int d) { return d == 0 ? cudaSuccess : 1; }
 inline cudaError_t cudaGetDeviceProperties(cudaDeviceProp* p, int) {
   std::memset(p, 0, sizeof(*p));
   std::strcpy(p->name, "SIMT emulation");

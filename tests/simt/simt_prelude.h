@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <algorithm>
 #include <thread>
 
 #define GPO_SIMT_EMU 1
@@ -26,6 +27,7 @@
 #define __device__
 #define __host__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 #define __launch_bounds__(...)
 #define __shared__
 #define __align__(n) __attribute__((aligned(n)))
@@ -94,6 +96,13 @@ inline unsigned long long __shfl_down_sync(unsigned, unsigned long long v, unsig
   const int src = lane + static_cast<int>(d) < 32 ? lane + static_cast<int>(d) : lane;
   return simt_gather(v, src);
 }
+inline unsigned long long __shfl_sync(unsigned, unsigned long long v, int src) {
+  return simt_gather(v, src);
+}
+inline int __shfl_sync(unsigned, int v, int src) {
+  return static_cast<int>(static_cast<unsigned>(simt_gather(static_cast<unsigned>(v), src)));
+}
+inline void __syncwarp(unsigned = 0xffffffffu) { simt_warp->bar->arrive_and_wait(); }
 inline void __syncthreads() { simt_block->arrive_and_wait(); }
 inline void __threadfence() { __atomic_thread_fence(__ATOMIC_SEQ_CST); }
 inline void __nanosleep(unsigned) { std::this_thread::yield(); }
@@ -102,6 +111,9 @@ inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
 inline int __ffs(int x) { return __builtin_ffs(x); }
 inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+inline int __clz(int x) { return x ? __builtin_clz(static_cast<unsigned>(x)) : 32; }
+using std::min;
+using std::max;
 inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
   return static_cast<unsigned long long>((static_cast<unsigned __int128>(a) * b) >> 64);
 }

@@ -1,9 +1,10 @@
 """The batched search kernel's own source (csrc/batched.cu) run on CPU
 threads under the SIMT emulation (tests/batched_emu.cpp,
 tests/simt/simt_prelude.h) against the reference's golden scores and the
-oracle: the frame tiers, the ordering threshold, the transposition table,
-in-kernel donation between warps, node budgets and input rejection -- the
-code paths a GPU run takes, checked without a GPU."""
+oracle: the frame placements, the ordering threshold, the transposition
+table, the stability cutoff, helping between the lanes of a warp, node
+budgets and input rejection -- the code paths a GPU run takes, checked
+without a GPU."""
 import ctypes
 
 import numpy as np
@@ -15,10 +16,10 @@ OVERLAP, DEPTH, BUDGET = 2, 1, 4
 
 
 class EmuOptions(ctypes.Structure):
-    _fields_ = [("warps", ctypes.c_int), ("ff", ctypes.c_int), ("smem_slots", ctypes.c_int),
-                ("donate_min", ctypes.c_int), ("long_nodes", ctypes.c_uint64),
-                ("max_tasks", ctypes.c_uint), ("node_budget", ctypes.c_uint64),
-                ("budget_mark", ctypes.c_int), ("tt_bits", ctypes.c_int),
+    _fields_ = [("warps", ctypes.c_int), ("ff", ctypes.c_int), ("shared_frames", ctypes.c_int),
+                ("help_min", ctypes.c_int), ("roots_per_warp", ctypes.c_int),
+                ("stab_min", ctypes.c_int), ("stab_gate", ctypes.c_int),
+                ("node_budget", ctypes.c_uint64), ("tt_bits", ctypes.c_int),
                 ("tt_min", ctypes.c_int), ("root_lists", ctypes.c_void_p),
                 ("learned_min", ctypes.c_int)]
 
@@ -55,7 +56,7 @@ def c1():
 
 def test_scores_and_best_moves(emu, oracle, c1):
     p, o, scores = c1
-    sc, bm, nodes, st = emu(p, o, 10, smem_slots=4)
+    sc, bm, nodes, st = emu(p, o, 10, shared_frames=1)
     assert np.array_equal(sc.astype(int), scores)
     assert st[6] == 0 and st[0] == nodes.sum() and (nodes > 0).all()
     # every best move reaches the score
@@ -70,54 +71,69 @@ def test_scores_and_best_moves(emu, oracle, c1):
         assert -int(v[0]) == int(sc[i])
 
 
-@pytest.mark.parametrize("ff,slots", [(8, 0), (11, 9)])
-def test_ordering_threshold_and_frame_tiers(emu, c1, ff, slots):
+@pytest.mark.parametrize("ff,shared", [(8, 0), (11, 1), (4, 1)])
+def test_ordering_threshold_and_frame_placement(emu, c1, ff, shared):
     p, o, scores = c1
-    sc, _, _, st = emu(p, o, 16, ff=ff, smem_slots=slots)
+    sc, _, _, st = emu(p, o, 16, ff=ff, shared_frames=shared)
     assert np.array_equal(sc.astype(int), scores) and st[6] == 0
 
 
 def test_transposition_table(emu, c1):
     p, o, scores = c1
-    sc, _, nodes, st = emu(p, o, 10, smem_slots=4, tt_bits=16, tt_min=6)
+    sc, _, nodes, st = emu(p, o, 10, shared_frames=1, tt_bits=16, tt_min=6)
     assert np.array_equal(sc.astype(int), scores) and st[6] == 0
     probes, hits, updates = int(st[1]), int(st[2]), int(st[3])
     assert probes > 0 and updates > 0 and hits <= probes
 
 
-def test_donation_between_warps(emu, oracle):
-    p, o = oracle.generate(11, 6, 13, 13)
-    want, _, _, _ = oracle.solve_batch(p, o, mode=1)
-    # 2 warps, 6 positions: idle lanes ask for subtrees; roots past 2048
-    # nodes hand moves out unasked
-    sc, _, nodes, st = emu(p, o, 13, warps=2, smem_slots=4, donate_min=8, long_nodes=2048)
-    assert np.array_equal(sc, want) and st[6] == 0
-    assert st[4] > 0  # subtrees handed out
-    assert st[0] == nodes.sum()
-
-
-def test_node_budget_marks_or_fails(emu, c1):
+def test_stability_cutoff(emu, c1):
     p, o, scores = c1
-    _, _, full_nodes, _ = emu(p, o, 10, smem_slots=4)
+    sc, _, _, st = emu(p, o, 10, shared_frames=1, stab_min=5, stab_gate=-64)
+    assert np.array_equal(sc.astype(int), scores) and st[6] == 0
+    assert st[5] > 0  # nodes closed by the cutoff
+
+
+@pytest.mark.parametrize("rpw,warps,shared", [(1, 1, 1), (3, 2, 0)])
+def test_helping_inside_a_warp(emu, oracle, rpw, warps, shared):
+    p, o = oracle.generate(11, 8, 11, 13)
+    want, _, _, _ = oracle.solve_batch(p, o, mode=1)
+    # few positions per warp: the idle lanes receive moves of split nodes
+    sc, bm, nodes, st = emu(p, o, 13, warps=warps, shared_frames=shared, help_min=6,
+                            roots_per_warp=rpw, tt_bits=16, tt_min=7, stab_min=6, stab_gate=10)
+    assert np.array_equal(sc, want) and st[6] == 0
+    assert st[4] > 0  # moves handed out
+    assert st[0] == nodes.sum()
+    # best moves stay optimal although helpers report most of the root's moves
+    for i in range(len(p)):
+        m = int(bm[i]) & 0xFF
+        if m >= 64:
+            continue
+        f = oracle.L.orc_flip(int(p[i]), int(o[i]), m)
+        cp, co = int(o[i]) ^ f, int(p[i]) ^ f ^ (1 << m)
+        v, _, _, _ = oracle.solve_batch(np.array([cp], np.uint64), np.array([co], np.uint64),
+                                        mode=1)
+        assert -int(v[0]) == int(sc[i])
+
+
+def test_node_budget_fails(emu, c1):
+    p, o, scores = c1
+    _, _, full_nodes, _ = emu(p, o, 10, shared_frames=1)
     budget = int(np.median(full_nodes))
-    sc, _, _, st = emu(p, o, 10, smem_slots=4, node_budget=budget, budget_mark=1)
-    over = sc == -128
-    assert over.any() and (~over).any() and st[6] == 0
-    assert np.array_equal(sc[~over].astype(int), scores[~over])
-    assert (full_nodes[over] > budget).all()
-    _, _, _, st = emu(p, o, 10, smem_slots=4, node_budget=budget)
+    _, _, _, st = emu(p, o, 10, shared_frames=1, node_budget=budget)
     assert int(st[6]) & BUDGET
+    _, _, _, st = emu(p, o, 10, shared_frames=1, node_budget=int(full_nodes.max()) + 1)
+    assert int(st[6]) == 0
 
 
 def test_rejected_inputs(emu, c1):
     p, o, scores = c1
     p, o = p[:8].copy(), o[:8].copy()
     p[3] |= np.uint64(int(o[3]) & -int(o[3]))  # a square in both bitboards
-    sc, _, _, st = emu(p, o, 10, smem_slots=4)
+    sc, _, _, st = emu(p, o, 10, shared_frames=1)
     assert int(st[6]) & OVERLAP and sc[3] == 0
     keep = np.arange(8) != 3
     assert np.array_equal(sc[keep].astype(int), scores[:8][keep])
-    _, _, _, st = emu(p[keep], o[keep], 9, smem_slots=4)
+    _, _, _, st = emu(p[keep], o[keep], 9, shared_frames=1)
     assert int(st[6]) & DEPTH
 
 
@@ -151,6 +167,6 @@ def test_learned_root_lists_keep_scores_exact(emu, oracle, c1, order):
                 moves.insert(0, int(b[0]))
         lists[i] = pack_root_list(moves, len(moves))
         used += 1
-    sc, bm, _, st = emu(p, o, 10, smem_slots=4, root_lists=lists.ctypes.data, learned_min=10)
+    sc, bm, _, st = emu(p, o, 10, shared_frames=1, root_lists=lists.ctypes.data, learned_min=10)
     assert used == len(p)
     assert np.array_equal(sc.astype(int), scores) and st[6] == 0

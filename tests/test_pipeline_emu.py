@@ -1,6 +1,6 @@
 """The library's whole solve pipeline -- C ABI, bucketing, batched and plain
-search kernels, expansion of hard positions into children and their
-combination, the allocation-free entry point, the generator -- compiled as
+search kernels, helping between the lanes of a warp, the allocation-free
+entry point, the generator -- compiled as
 host C++ and run on CPU threads (tests/pipeline_emu.cpp under the SIMT
 emulation), called through the same C ABI the product exports, against the
 reference's golden scores and the oracle.  No GPU is involved; this checks
@@ -37,6 +37,7 @@ def solve(L, p, o, depth, **kw):
     opt = g.Options()
     L.gpo_default_options(ctypes.byref(opt))
     opt.threads_per_block = 32
+    opt.table_bits = 16  # a small table keeps the emulated clears cheap
     for k, v in kw.items():
         setattr(opt, k, v)
     st = g.Stats()
@@ -71,27 +72,30 @@ def test_default_pass(emu, oracle, c1):
     p, o, scores = c1
     rc, sc, bm, nodes, st = solve(emu, p, o, 10)
     assert rc == 0 and np.array_equal(sc.astype(int), scores)
-    # bucketing (3), the search, the marking pass that finds nothing
-    assert st.launches == 5 and st.splits == 0
+    # bucketing (3) and one search launch: no host round trip in between
+    assert st.launches == 4
     assert st.nodes == int(nodes.sum())
+    assert st.table_probes > 0  # the table is on by default
     best_moves_reach_scores(oracle, p, o, sc, bm)
 
 
-def test_expansion_of_hard_positions(emu, oracle, c1):
-    p, o, scores = c1
-    rc, sc, bm, nodes, st = solve(emu, p, o, 10, expand_budget=3000)
-    assert rc == 0 and np.array_equal(sc.astype(int), scores)
-    assert st.splits > 0            # child positions made
-    assert st.launches > 5          # further passes, expansion and combination
+def test_helping_on_few_positions(emu, oracle):
+    """Few deep positions for the warp: one root per warp, the other lanes
+    search moves of its split nodes."""
+    p, o = oracle.generate(12, 3, 12, 13)
+    want, _, _, _ = oracle.solve_batch(p, o, mode=1)
+    rc, sc, bm, nodes, st = solve(emu, p, o, 13, roots_per_warp=1, help_min_empties=6)
+    assert rc == 0 and np.array_equal(sc, want)
+    assert st.splits > 0 and st.nodes == int(nodes.sum())
     best_moves_reach_scores(oracle, p, o, sc, bm)
 
 
-def test_expansion_on_mixed_empties(emu):
+def test_mixed_empties_without_shared_frames(emu):
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
     small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 11
     p, o, scores = p[small][:40], o[small][:40], scores[small][:40]
-    rc, sc, _, _, st = solve(emu, p, o, 16, expand_budget=2000, smem_frames=-1)
-    assert rc == 0 and np.array_equal(sc.astype(int), scores) and st.splits > 0
+    rc, sc, _, _, st = solve(emu, p, o, 16, smem_frames=-1)
+    assert rc == 0 and np.array_equal(sc.astype(int), scores)
 
 
 def test_plain_kernel_walks_reference_tree(emu, oracle, c1):
@@ -103,14 +107,18 @@ def test_plain_kernel_walks_reference_tree(emu, oracle, c1):
 
 
 @pytest.mark.parametrize("kw", [{"use_table": 1, "table_bits": 16, "table_min_empties": 6},
-                                {"split_min_empties": 8, "threads_per_block": 64},
+                                {"use_table": 0, "stability_min_empties": -1,
+                                 "help_min_empties": -1},
+                                {"roots_per_warp": 4, "threads_per_block": 64},
                                 {"fastest_first_empties": 11, "smem_frames": 3}])
 def test_options_keep_scores_exact(emu, c1, kw):
     p, o, scores = c1
     rc, sc, _, _, st = solve(emu, p, o, 12, **kw)
     assert rc == 0 and np.array_equal(sc.astype(int), scores)
-    if "use_table" in kw:
+    if kw.get("use_table") == 1:
         assert st.table_probes > 0 and st.table_updates > 0
+    if kw.get("use_table") == 0:
+        assert st.table_probes == 0
 
 
 def test_error_statuses(emu, c1):
@@ -122,8 +130,11 @@ def test_error_statuses(emu, c1):
     assert rc == g.GPO_ERR_BOARD
     keep = np.arange(len(p)) != 5
     assert np.array_equal(sc[keep].astype(int), scores[keep])
-    # a node budget without splitting fails instead of marking
-    assert solve(emu, p, o, 10, node_budget=500, split_min_empties=-1)[0] == g.GPO_ERR_TIMEOUT
+    # the node budget is a watchdog: exceeding it fails the call
+    assert solve(emu, p, o, 10, node_budget=500)[0] == g.GPO_ERR_TIMEOUT
+    # bad option values
+    assert solve(emu, p, o, 10, roots_per_warp=33)[0] == g.GPO_ERR_ARG
+    assert solve(emu, p, o, 10, table_bits=40)[0] == g.GPO_ERR_ARG
 
 
 def test_allocation_free_entry_point(emu, c1):
@@ -157,47 +168,17 @@ def test_random_option_mixes(emu, oracle):
         want, _, _, _ = oracle.solve_batch(p, o, mode=1)
         kw = {"threads_per_block": int(rng.choice([32, 64]))}
         if rng.random() < 0.5:
-            kw["expand_budget"] = int(rng.choice([50, 300, 2000]))
+            kw["roots_per_warp"] = int(rng.choice([1, 2, 8]))
+        if rng.random() < 0.5:
+            kw["help_min_empties"] = int(rng.choice([-1, 4, 6, 9]))
         if rng.random() < 0.3:
-            kw["split_min_empties"] = int(rng.choice([-1, 6, 9]))
+            kw.update(use_table=int(rng.choice([0, 1])),
+                      table_min_empties=int(rng.integers(3, 10)))
         if rng.random() < 0.3:
-            kw.update(use_table=1, table_bits=16, table_min_empties=int(rng.integers(4, 10)))
+            kw["stability_min_empties"] = int(rng.choice([-1, 3, 6]))
         if rng.random() < 0.3:
             kw["smem_frames"] = int(rng.choice([-1, 1, 3, 8]))
         if rng.random() < 0.3:
-            kw["fastest_first_empties"] = int(rng.integers(4, 13))
+            kw["fastest_first_empties"] = int(rng.integers(3, 13))
         rc, sc, _, _, _ = solve(emu, p, o, depth, **kw)
         assert rc == 0 and np.array_equal(sc, want), (n, lo, hi, depth, kw)
-
-
-@pytest.mark.parametrize("mode", [1, 2])
-def test_windowed_expansion_is_exact_and_smaller(emu, oracle, mode):
-    """expand_windows = 1 (principal variation first at the top) and 2 (at
-    every expanded position): same scores, optimal best moves, fewer nodes
-    than full-window children."""
-    p, o, scores, _ = golden_ref("c3_seed2_mixed")
-    small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 10
-    p, o, scores = p[small][:32], o[small][:32], scores[small][:32]
-    _, _, _, _, full = solve(emu, p, o, 16, expand_budget=500)
-    rc, sc, bm, nodes, st = solve(emu, p, o, 16, expand_budget=500, expand_windows=mode)
-    assert rc == 0 and np.array_equal(sc.astype(int), scores)
-    best_moves_reach_scores(oracle, p, o, sc, bm)
-    assert st.nodes == int(nodes.sum())
-    assert st.nodes < full.nodes
-
-
-def test_windowed_expansion_random_batches(emu, oracle):
-    rng = np.random.default_rng(77)
-    for _ in range(6):
-        n = int(rng.integers(1, 20))
-        lo = int(rng.integers(4, 11))
-        hi = int(rng.integers(lo, 12))
-        p, o = oracle.generate(int(rng.integers(100, 10000)), n, lo, hi)
-        want, _, _, _ = oracle.solve_batch(p, o, mode=1)
-        kw = {"expand_windows": int(rng.choice([1, 2])),
-              "expand_budget": int(rng.choice([30, 200, 1500]))}
-        if rng.random() < 0.4:
-            kw.update(use_table=1, table_bits=16, table_min_empties=6)
-        rc, sc, bm, _, _ = solve(emu, p, o, hi + int(rng.integers(0, 4)), **kw)
-        assert rc == 0 and np.array_equal(sc, want), kw
-        best_moves_reach_scores(oracle, p, o, sc, bm)
