@@ -7,19 +7,15 @@ chosen per GPU and workload by timing candidates on a bounded sample of the
 caller's batch:
 
   threads_per_block      block width of the persistent search grid
-  smem_frames            stack placement: the shared-memory frame tier
-                         (0 = the largest that keeps occupancy, -1 = every
-                         frame in the global array)
+  smem_frames            stack placement: frames in shared memory when they
+                         fit (0) or every frame in the global array (-1)
   fastest_first_empties  the empty count from which moves are ordered by
                          the opponent's reply count
-  expand_budget          the split threshold of hard positions: the node
-                         budget after which a position is replaced by its
-                         children in the next pass
-  expand_windows         how those children are searched: all with full
-                         windows, or principal variation first (at the top
-                         level, or at every expanded position)
-  use_table              the transposition table (2^24 entries), which also
-                         carries work between the expansion's passes
+  table_min_empties      the empty count from which nodes use the
+                         transposition table
+  help_min_empties       the warp-split threshold: the empty count a node
+                         needs before idle lanes of its warp take its moves
+                         (-1 = no helping)
 
 Search: coordinate descent from the library defaults, one parameter at a
 time, each candidate timed on the same sample (best of `repeats` runs).
@@ -38,19 +34,17 @@ import numpy as np
 DEFAULTS = {
     "threads_per_block": 128,
     "smem_frames": 0,
-    "fastest_first_empties": 9,
-    "expand_budget": 1 << 22,
-    "expand_windows": 0,
-    "use_table": 0,
+    "fastest_first_empties": 6,
+    "table_min_empties": 7,
+    "help_min_empties": 7,
 }
 
 SPACE = (
     ("threads_per_block", (64, 128, 256)),
     ("smem_frames", (0, -1)),
-    ("fastest_first_empties", (8, 9, 10, 11)),
-    ("expand_budget", (1 << 20, 1 << 22, 1 << 24)),
-    ("expand_windows", (0, 1, 2)),
-    ("use_table", (0, 1)),
+    ("fastest_first_empties", (5, 6, 7, 8)),
+    ("table_min_empties", (6, 7, 8, 9)),
+    ("help_min_empties", (6, 7, 9, -1)),
 )
 
 

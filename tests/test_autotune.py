@@ -10,14 +10,12 @@ from gpuothello2_gb300 import autotune as at
 
 
 def synthetic_cost(params):
-    # separable, minimum at threads 256, smem -1, ff 10, budget 2^20, windows 1,
-    # table on
+    # separable, minimum at threads 256, smem -1, ff 8, table from 9, help from 6
     t = {64: 3.0, 128: 2.0, 256: 1.0}[params["threads_per_block"]]
     t += {0: 0.5, -1: 0.0}[params["smem_frames"]]
-    t += abs(params["fastest_first_empties"] - 10) * 0.25
-    t += {1 << 20: 0.0, 1 << 22: 0.1, 1 << 24: 0.2}[params["expand_budget"]]
-    t += {0: 0.05, 1: 0.0, 2: 0.02}[params["expand_windows"]]
-    t += {0: 0.01, 1: 0.0}[params["use_table"]]
+    t += abs(params["fastest_first_empties"] - 8) * 0.25
+    t += abs(params["table_min_empties"] - 9) * 0.1
+    t += {6: 0.0, 7: 0.05, 9: 0.1, -1: 0.2}[params["help_min_empties"]]
     return t
 
 
@@ -29,8 +27,8 @@ def test_coordinate_descent_finds_the_separable_minimum():
         return synthetic_cost(prm), np.zeros(4, np.int8)
 
     best, t, hist = at.coordinate_descent(measure)
-    assert best == {"threads_per_block": 256, "smem_frames": -1, "fastest_first_empties": 10,
-                    "expand_budget": 1 << 20, "expand_windows": 1, "use_table": 1}
+    assert best == {"threads_per_block": 256, "smem_frames": -1, "fastest_first_empties": 8,
+                    "table_min_empties": 9, "help_min_empties": 6}
     assert t == pytest.approx(synthetic_cost(best))
     # the start plus every other value of every parameter, each timed once
     assert len(calls) == 1 + sum(len(v) - 1 for _, v in at.SPACE)
@@ -50,7 +48,7 @@ def test_repeats_keep_the_fastest_run():
 def test_a_parameter_that_changes_a_score_stops_tuning():
     def measure(prm):
         s = np.array([2, -4, 0], np.int8)
-        if prm["fastest_first_empties"] == 11:
+        if prm["fastest_first_empties"] == 8:
             s[1] = -6
         return 1.0, s
 

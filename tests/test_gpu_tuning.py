@@ -1,5 +1,5 @@
 """Autotuner on the GPU: every candidate parameter set (block width, frame
-placement, fastest-first threshold, expansion budget) solves the sample
+placement, fastest-first threshold, warp-split threshold) solves the sample
 with identical scores, the winners are cached, and the tuned options give
 the oracle's scores on the whole batch."""
 import numpy as np
@@ -12,10 +12,9 @@ pytestmark = pytest.mark.gpu
 
 SPACE = (
     ("threads_per_block", (64, 128, 256)),
-    ("smem_frames", (0, 4, -1)),
-    ("fastest_first_empties", (8, 9, 11)),
-    # 2^16 nodes makes the harder 14-empty positions expand into children
-    ("expand_budget", (1 << 16, 1 << 22)),
+    ("smem_frames", (0, -1)),
+    ("fastest_first_empties", (5, 6, 9)),
+    ("help_min_empties", (6, -1)),
 )
 
 
@@ -38,7 +37,7 @@ def test_tuned_parameters_keep_scores_exact(gpu, oracle, tmp_path):
     assert st.launches >= 4
 
 
-@pytest.mark.parametrize("smem_frames", [-1, 3])
+@pytest.mark.parametrize("smem_frames", [-1, 0])
 @pytest.mark.parametrize("threads", [64, 256])
 def test_frame_placement_and_block_width_on_reference_scores(gpu, threads, smem_frames):
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
