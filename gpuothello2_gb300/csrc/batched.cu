@@ -27,7 +27,8 @@
 //     (solver.cu:57-73, 214-221, 246-256 semantics).
 //
 // Uniform step.  Every loop iteration every lane does at most one move flip
-// plus one mobility (or, at nodes with two empties, one or two more flips):
+// plus one mobility (or, at nodes with two empties, the child's last-square
+// flip counts from two small table lookups per line):
 // a move (the child is pushed), a fastest-first ordering probe, a root init,
 // a pass, a re-mask, or a handed-out move.  Only the bookkeeping around it
 // diverges.  The loop keeps one copy of the flip and of the mobility code,
@@ -70,7 +71,9 @@ namespace {
 enum : int { OP_NONE = 0, OP_INIT, OP_MOVE, OP_PASS, OP_KEY, OP_REMASK, OP_HAND };
 enum : int { PH_INIT = 0, PH_MASK, PH_KEY, PH_LIST };
 
-constexpr int kRayBytes = 256 * 8;
+// shared tables: 64 x 4 up-rays (flip), 64 x 2 diagonal masks and the
+// 8 x 256 last-square flip counts (bitboard.cuh)
+constexpr int kTableBytes = (256 + 128) * 8 + 8 * 256;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr u64 kResearch = 1ULL;  // flips-word flag: the child is a re-search
 
@@ -235,9 +238,11 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
   extern __shared__ __align__(16) u64 smem_raw[];
   const int B = blockDim.x;
   const int t = threadIdx.x;
-  u64* const rays = smem_raw;  // 64 x 4 up-ray table (bitboard.cuh)
+  u64* const rays = smem_raw;         // 64 x 4 up-rays (bitboard.cuh)
+  u64* const dmask = smem_raw + 256;  // 64 x 2 diagonal masks
+  unsigned char* const lcnt = reinterpret_cast<unsigned char*>(smem_raw + 384);  // 8 x 256 counts
   SplitState sp;
-  sp.P = smem_raw + 256;
+  sp.P = smem_raw + kTableBytes / 8;
   sp.O = sp.P + B;
   sp.pend = reinterpret_cast<unsigned*>(sp.O + B);
   sp.acc = sp.pend + B;
@@ -246,6 +251,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
   sp.beta = sp.lo + B;
   u64* const fbase = reinterpret_cast<u64*>(sp.beta + B);  // B is a multiple of 32: aligned
   gpo_build_rays(rays);
+  gpo_build_last(lcnt, dmask);
   sp.pend[t] = 0;
   sp.acc[t] = 0;
   sp.cut[t] = 0;
@@ -603,41 +609,18 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
     const u64 X = op == OP_HAND ? hX : P;
     const u64 Y = op == OP_HAND ? hY : O;
     const u64 bit = play ? (1ULL << sq) : 0ULL;
-    // One flip site for up to three flips: the move; then, at a node with
-    // two empties, the child's last square s for the child, and for its
-    // opponent if the child cannot play it.
-    u64 f = 0, cP = X, cO = Y, fa = X, fb = Y;
-    int fs = sq, s1 = 0, n1 = 0;
-    bool fon = play;
-#pragma unroll 1
-    for (int k = 0;; ++k) {
-      // fs & 63: a lane that skips this flip may hold no square (-1)
-      const u64 r = fon ? gpo_flip(fa, fb, fs & 63, rays) : 0ULL;
-      if (k == 0) {
-        f = r;
-        cP = same ? X : (Y ^ f);
-        cO = same ? Y : (X ^ f ^ bit);
-        fa = cP;
-        fb = cO;
-        fs = ctz64(~(cP | cO));
-        fon = fold;
-      } else if (k == 1) {
-        n1 = popc(r);
-        fa = cO;
-        fb = cP;
-        fon = fold && n1 == 0;
-      } else {
-        // the child (cP to move) plays s if it can, else cO does, else the
-        // game ends with s empty
-        const int n2 = popc(r);
-        s1 = n1 ? 2 * (popc(cP) + n1 + 1) - 64
-                : (n2 ? 64 - 2 * (popc(cO) + n2 + 1) : gpo_final(cP, cO));
-        break;
-      }
-      if (!__any_sync(kFull, fon)) {
-        if (k == 1 && fold) s1 = 2 * (popc(cP) + n1 + 1) - 64;  // n1 > 0 here
-        break;
-      }
+    const u64 f = play ? gpo_flip(X, Y, sq, rays) : 0ULL;
+    const u64 cP = same ? X : (Y ^ f);
+    const u64 cO = same ? Y : (X ^ f ^ bit);
+    int s1 = 0;
+    if (__any_sync(kFull, fold)) {
+      // the child (cP to move) has one empty square s: it plays s if it can,
+      // else cO does, else the game ends with s empty
+      const int s = ctz64(~(cP | cO)) & 63;  // & 63: lanes without a fold may hold none
+      const int n1 = gpo_last_count(cP, s, lcnt, dmask);
+      const int n2 = gpo_last_count(cO, s, lcnt, dmask);
+      s1 = n1 ? 2 * (popc(cP) + n1 + 1) - 64
+              : (n2 ? 64 - 2 * (popc(cO) + n2 + 1) : gpo_final(cP, cO));
     }
     u64 cm = 0;
     if (__any_sync(kFull, needmob)) cm = gpo_mobility(cP, cO);
@@ -785,7 +768,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
 
 size_t batched_smem_bytes(int threads, int smem_top) {
   const int sslots = smem_top >= 3 ? smem_top - 2 : 0;
-  return kRayBytes + static_cast<size_t>(threads) * (kSplitBytes + sslots * kFrameBytes);
+  return kTableBytes + static_cast<size_t>(threads) * (kSplitBytes + sslots * kFrameBytes);
 }
 
 cudaError_t batched_grid(int threads, int smem_top, int sms, int* grid, size_t* smem) {
@@ -814,7 +797,7 @@ cudaError_t batched_plan(int threads, int depth, int* smem_top) {
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   // 1 KB per block is reserved by the hardware
-  const long per_block = static_cast<long>(smem_sm) / per_sm - 1024 - kRayBytes -
+  const long per_block = static_cast<long>(smem_sm) / per_sm - 1024 - kTableBytes -
                          static_cast<long>(threads) * kSplitBytes;
   const long need = static_cast<long>(depth > 2 ? depth - 2 : 0) * threads * kFrameBytes;
   *smem_top = need <= per_block ? depth : 2;

@@ -102,6 +102,65 @@ __device__ __forceinline__ int gpo_final(u64 P, u64 O) {
   return pc == oc ? 0 : (pc > oc ? 64 - 2 * oc : 2 * pc - 64);
 }
 
+// ---- flip counts at the last empty square ----
+// With one empty square s, every other square holds a disc, so along each
+// line through s the discs of one side are the complement of the other's:
+// the discs X flips by playing s follow from X's 8-bit pattern on the line
+// alone (the runs of non-X squares next to s that end at an X disc).
+// cnt[pos * 256 + x] holds that count for an 8-square line with X pattern x
+// and s at position pos.  The lines are gathered into 8-bit patterns:
+//   row:       bit c = square (r, c);
+//   column:    ((X >> c) & 0x0101..01) * 0x0102040810204080 >> 56, bit k =
+//              square (k, c) (the partial products land on distinct bits);
+//   diagonals: (X & mask) * 0x0101..01 >> 56, bit c = the diagonal's square
+//              in column c.
+// A diagonal shorter than 8 squares reads 0 (not X) past its ends, which is
+// harmless: a run reaching past the board edge ends at no X disc.
+// dmask[2 * s] / dmask[2 * s + 1]: the squares of s's a1-h8 and a8-h1
+// diagonals.  Both tables are built once per block (gpo_build_last).
+__device__ __forceinline__ void gpo_build_last(unsigned char* cnt, u64* dmask) {
+  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) {
+    const int pos = i >> 8, x = i & 255;
+    int n = 0, k = 0;
+    for (int j = pos + 1; j < 8; ++j) {  // toward higher positions
+      if ((x >> j) & 1) {
+        n += k;
+        break;
+      }
+      ++k;
+    }
+    k = 0;
+    for (int j = pos - 1; j >= 0; --j) {  // toward lower positions
+      if ((x >> j) & 1) {
+        n += k;
+        break;
+      }
+      ++k;
+    }
+    cnt[i] = static_cast<unsigned char>(n);
+  }
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    const int sq = i >> 1, r = sq >> 3, c = sq & 7;
+    u64 m = 0;
+    for (int rr = 0; rr < 8; ++rr) {
+      const int cc = (i & 1) ? (r + c - rr) : (c - r + rr);  // a8-h1 : a1-h8
+      if (cc >= 0 && cc < 8) m |= 1ULL << (rr * 8 + cc);
+    }
+    dmask[i] = m;
+  }
+}
+
+__device__ __forceinline__ int gpo_last_count(u64 X, int s, const unsigned char* cnt,
+                                              const u64* dmask) {
+  const int r = s >> 3, c = s & 7;
+  const unsigned row = static_cast<unsigned>(X >> (8 * r)) & 0xffu;
+  const unsigned col =
+      static_cast<unsigned>((((X >> c) & 0x0101010101010101ULL) * 0x0102040810204080ULL) >> 56);
+  const unsigned d9 = static_cast<unsigned>(((X & dmask[2 * s]) * 0x0101010101010101ULL) >> 56);
+  const unsigned d7 = static_cast<unsigned>(((X & dmask[2 * s + 1]) * 0x0101010101010101ULL) >> 56);
+  return cnt[c * 256 + row] + cnt[r * 256 + col] + cnt[c * 256 + d9] + cnt[c * 256 + d7];
+}
+
 // ---- stable discs ----
 // A subset of the discs of `O` that no sequence of moves can flip: a disc is
 // kept when, along each of the four line directions, its line is full, it

@@ -25,7 +25,7 @@ std::mutex simt_cas128_mutex;
 namespace gpo {
 // dynamic shared memory of the one emulated block: the ray table, the
 // split-node state and up to 30 frame slots for 128 threads
-constexpr size_t kEmuSmemWords = (kRayBytes + 128 * (kSplitBytes + 30 * kFrameBytes)) / 8 + 8;
+constexpr size_t kEmuSmemWords = (kTableBytes + 128 * (kSplitBytes + 30 * kFrameBytes)) / 8 + 8;
 alignas(16) u64 smem_raw[kEmuSmemWords];
 }  // namespace gpo
 

@@ -39,7 +39,7 @@ namespace gpo {
 // dynamic shared memory of a block of the batched kernel (blocks of a launch
 // run one after another): the ray table, the split-node state and up to 30
 // frame slots for 256 threads
-constexpr size_t kEmuSmemWords = (kRayBytes + 256 * (kSplitBytes + 30 * kFrameBytes)) / 8 + 8;
+constexpr size_t kEmuSmemWords = (kTableBytes + 256 * (kSplitBytes + 30 * kFrameBytes)) / 8 + 8;
 alignas(16) u64 smem_raw[kEmuSmemWords];
 
 // the learned orderer is not part of this build
