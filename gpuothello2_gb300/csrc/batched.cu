@@ -76,6 +76,11 @@ enum : int { PH_INIT = 0, PH_MASK, PH_KEY, PH_LIST };
 constexpr int kTableBytes = (256 + 128) * 8 + 8 * 256;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr u64 kResearch = 1ULL;  // flips-word flag: the child is a re-search
+// Levels a lane may return through per iteration.  A lane finishing a deep
+// subtree can return through several levels at once; every extra level is
+// another pass of the warp through the return code, so a lane with more to
+// return continues in the next iteration instead.
+constexpr int kMaxPops = 2;
 
 __device__ __forceinline__ unsigned pack_meta(int sq, int alpha, int beta, int best, int passed,
                                               int list) {
@@ -156,11 +161,12 @@ __device__ __forceinline__ int nth_bit(unsigned m, int k) {
   return __ffs(static_cast<int>(m)) - 1;
 }
 
-// ---- rare paths, kept out of line so that the hot loop stays small ----
+// ---- table access, and the rare paths kept out of line so that the hot
+//      loop stays small ----
 
 // Table bounds of (P, O): 0 = not found, else 1 << 16 | (lower + 64) << 8 |
 // (upper + 64).
-__device__ __noinline__ unsigned tt_lookup(unsigned long long* tt, int bits, u64 P, u64 O) {
+__device__ __forceinline__ unsigned tt_lookup(unsigned long long* tt, int bits, u64 P, u64 O) {
   int lb, ub;
   if (!tt_probe(tt, bits, tt_key(P, O), lb, ub)) return 0u;
   return (1u << 16) | (static_cast<unsigned>(lb + 64) << 8) | static_cast<unsigned>(ub + 64);
@@ -169,7 +175,7 @@ __device__ __noinline__ unsigned tt_lookup(unsigned long long* tt, int bits, u64
 // Stores the bound a closed node proves: best >= beta proves value >= best,
 // anything lower proves value <= best (an exact value is also an upper
 // bound).  Returns 1 if stored.
-__device__ __noinline__ int tt_record(unsigned long long* tt, int bits, u64 P, u64 O, int best,
+__device__ __forceinline__ int tt_record(unsigned long long* tt, int bits, u64 P, u64 O, int best,
                                       int beta) {
   const TTKey k = tt_key(P, O);
   return best >= beta ? tt_store(tt, bits, k, best, 64) : tt_store(tt, bits, k, -64, best);
@@ -363,6 +369,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
     bool stall = false;
     if (busy) {
       if (phase != PH_INIT) {
+        int pops = 0;
         for (;;) {
           bool more;
           if (phase == PH_KEY) more = true;
@@ -450,6 +457,11 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
             helper = false;
             break;
           }
+          if (pops == kMaxPops) {  // more levels to return: next iteration
+            stall = true;
+            break;
+          }
+          ++pops;
           // back to the parent, unless this child must be searched again
           u64 m, f;
           unsigned meta;
