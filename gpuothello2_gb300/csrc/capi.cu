@@ -166,7 +166,7 @@ int status_to_error(unsigned st) {
 
 int check_options(const gpo_options* opt) {
   if (!opt) return GPO_OK;
-  if (opt->table_bits != 0 && (opt->table_bits < 16 || opt->table_bits > 32)) return GPO_ERR_ARG;
+  if (opt->table_bits != 0 && (opt->table_bits < 17 || opt->table_bits > 32)) return GPO_ERR_ARG;
   if (opt->method != GPO_METHOD_BATCHED && opt->method != GPO_METHOD_PLAIN) return GPO_ERR_ARG;
   // the batched kernel is compiled for at most 256 threads per block
   if (opt->threads_per_block != 0 &&

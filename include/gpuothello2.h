@@ -68,8 +68,8 @@ typedef struct gpo_options {
                                  that have >= this many empties (young brothers wait, after
                                  the node's first move); 0 = default (7), negative = off */
   int wait_limit_ms;          /* deadline of one search launch; 0 = 600000 */
-  int table_bits;             /* transposition table of 2^table_bits 16-byte entries
-                                 (16..32); 0 = 24 */
+  int table_bits;             /* transposition table of 2^table_bits 16-byte entries in
+                                 buckets of two (17..32); 0 = 24 */
   int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 7 */
   int smem_frames;            /* search frames (depth - 2 slots per lane) in shared memory:
                                  0 = when they all fit at the register-limited occupancy,

@@ -80,7 +80,7 @@ def test_ordering_threshold_and_frame_placement(emu, c1, ff, shared):
 
 def test_transposition_table(emu, c1):
     p, o, scores = c1
-    sc, _, nodes, st = emu(p, o, 10, shared_frames=1, tt_bits=16, tt_min=6)
+    sc, _, nodes, st = emu(p, o, 10, shared_frames=1, tt_bits=17, tt_min=6)
     assert np.array_equal(sc.astype(int), scores) and st[6] == 0
     probes, hits, updates = int(st[1]), int(st[2]), int(st[3])
     assert probes > 0 and updates > 0 and hits <= probes
@@ -99,7 +99,7 @@ def test_helping_inside_a_warp(emu, oracle, rpw, warps, shared):
     want, _, _, _ = oracle.solve_batch(p, o, mode=1)
     # few positions per warp: the idle lanes receive moves of split nodes
     sc, bm, nodes, st = emu(p, o, 13, warps=warps, shared_frames=shared, help_min=6,
-                            roots_per_warp=rpw, tt_bits=16, tt_min=7, stab_min=6, stab_gate=10)
+                            roots_per_warp=rpw, tt_bits=17, tt_min=7, stab_min=6, stab_gate=10)
     assert np.array_equal(sc, want) and st[6] == 0
     assert st[4] > 0  # moves handed out
     assert st[0] == nodes.sum()

@@ -37,7 +37,7 @@ def solve(L, p, o, depth, **kw):
     opt = g.Options()
     L.gpo_default_options(ctypes.byref(opt))
     opt.threads_per_block = 32
-    opt.table_bits = 16  # a small table keeps the emulated clears cheap
+    opt.table_bits = 17  # a small table keeps the emulated clears cheap
     for k, v in kw.items():
         setattr(opt, k, v)
     st = g.Stats()
@@ -106,7 +106,7 @@ def test_plain_kernel_walks_reference_tree(emu, oracle, c1):
     assert np.array_equal(nodes, onodes) and st.launches == 1
 
 
-@pytest.mark.parametrize("kw", [{"use_table": 1, "table_bits": 16, "table_min_empties": 6},
+@pytest.mark.parametrize("kw", [{"use_table": 1, "table_bits": 17, "table_min_empties": 6},
                                 {"use_table": 0, "stability_min_empties": -1,
                                  "help_min_empties": -1},
                                 {"roots_per_warp": 4, "threads_per_block": 64},
