@@ -23,12 +23,14 @@ the timed region.
   cpu_baseline  the oracle's restatement of the reference tree on all host
          cores, on a bounded sample of the same stream
 
-Options: `--learned` trains the MLP move orderer first (untimed) and orders
-the roots of positions with >= 14 empties with it; `--table` turns on the
-transposition table and reports its probes, hits, updates and 32-byte-sector
-traffic rate; `--tuned` autotunes the
-launch and search parameters on a sample of the batch first (untimed);
-`--plain` also times the plain kernel on the same batch.
+The transposition table is always on; the line reports its size, probes,
+hits, updates and 32-byte-sector traffic rate.  A stratified sample of the
+scores is checked against the oracle outside the timed region
+(`parity_sample`).  Options: `--learned` orders the top of the search with
+the learned move orderer (weights trained by the library's own GPU kernels,
+loaded from a file); `--tuned` autotunes the launch and search parameters on
+a sample of the batch first (untimed); `--plain` also times the plain kernel
+on the same batch; `--table-bits` sets the table size.
 
 `--impl reference` times the reference algorithm on the host cores instead
 (the oracle port of the reference tree; the reference's own search only
@@ -49,10 +51,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W_NODE = 418  # INT32 ops per node: mobility + flip + make-move of the reference arithmetic
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per position of
-# one batched-kernel launch, from one ncu capture of a 131,072-position launch
-# (2,711,552 B), scaled to the launch by its position count.
-DRAM_BYTES_PER_POSITION = 2711552.0 / 131072
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per search node
+# of one batched-kernel launch, from one ncu capture of a smaller launch
+# (profiles/batched_kernel_ncu.md), scaled to this launch by its node count:
+# the traffic is the transposition table's, which grows with the nodes.
+TRAFFIC_BYTES_PER_NODE = (4.026357e9 + 2.894098e9) / 3.639e9
+TRAFFIC_SOURCE = ("ncu capture of 131,072 positions x 12 empties (6.92 GB in 3.64e9 nodes), "
+                  "scaled by nodes")
 SEED, N_POS, LO, HI, DEPTH = 2, 1 << 20, 8, 16, 16
 METRIC = "exact-solved positions/s at 8\u201316 empties: batched+learned vs plain, same GB300"
 WORKLOAD = ("1,048,576 positions, random playouts seed 2, empties uniform 8..16, DEPTH 16")
@@ -196,6 +201,30 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def parity_sample(p, o, scores, threads=0):
+    """Scores of a stratified sample of the batch against the oracle's own
+    alpha-beta solver (orc_solve_fast: a different tree, same exact values),
+    outside the timed region: every 512th position of the batch (all empty
+    counts in proportion) plus the first 256 positions with 16 empties (the
+    hardest searches)."""
+    import numpy as np
+    from gpuothello2_gb300 import build as B
+    from tests.oracle_lib import Oracle
+
+    B.build_oracle()
+    orc = Oracle(B.ORACLE_LIB)
+    empties = 64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p[:1 << 16], o[:1 << 16])])
+    hard = np.nonzero(empties == HI)[0][:256]
+    idx = np.unique(np.concatenate([np.arange(0, len(p), 512), hard]))
+    t0 = time.perf_counter()
+    want, _, _, _ = orc.solve_batch(p[idx], o[idx], DEPTH, mode=1, threads=threads)
+    mism = int(np.sum(want.astype(int) != scores[idx].astype(int)))
+    return {"n": int(len(idx)), "mismatches": mism, "hard_16_empties": int(len(hard)),
+            "seconds": time.perf_counter() - t0,
+            "how": "every 512th position + the first 256 with 16 empties, against the oracle's "
+                   "own alpha-beta (orc_solve_fast), outside the timed region"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -205,21 +234,16 @@ def main():
     ap.add_argument("--plain", action="store_true",
                     help="also time the plain kernel on the same batch (minutes)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--n", type=int, default=N_POS)
-    ap.add_argument("--split", type=int, default=0,
-                    help="split_min_empties option (0 = library default, <0 = off)")
+    ap.add_argument("--table-bits", type=int, default=0,
+                    help="transposition table of 2^bits entries (0 = library default: 2^28 on "
+                         "a device with >= 64 GiB)")
     ap.add_argument("--learned", action="store_true",
-                    help="train the MLP move orderer first (untimed: solver-labelled positions "
-                         "of seed 3 at 12-14 empties, GPU training kernels) and order the roots "
-                         "of positions with >= 14 empties with it")
-    ap.add_argument("--learned-train", type=int, default=1 << 20,
-                    help="training positions for --learned")
-    ap.add_argument("--table", action="store_true",
-                    help="use the transposition table (2^24 16-byte entries, nodes with >= 11 "
-                         "empties) and report its traffic")
-    ap.add_argument("--windows", type=int, default=0, choices=[0, 1, 2],
-                    help="principal-variation-first expansion of hard positions: 1 = at the "
-                         "top level, 2 = at every expanded position (expand_windows)")
+                    help="order the top of the search with the learned move orderer "
+                         "(weights from --weights)")
+    ap.add_argument("--weights", default=os.path.join(ROOT, "gpuothello2_gb300", "data",
+                                                      "orderer.f32"))
     ap.add_argument("--tuned", action="store_true",
                     help="autotune launch/search parameters on a 4,096-position sample of the "
                          "batch first (untimed; cached per GPU, depth and empties range)")
@@ -255,15 +279,9 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     learned_info = None
     if args.learned:
-        t0 = time.perf_counter()
-        tp, to = g.generate(3, args.learned_train, 12, 14)
-        _, labels, _, _, _ = g.solve(tp, to, 14, best=True)
-        w, hist = g.mlp_train(tp, to, labels, g.mlp_init(3), epochs=4, batch=2048, lr=1e-3,
-                              seed=1)
+        w = np.fromfile(args.weights, dtype=np.float32)
         g.mlp_load(w)
-        learned_info = {"train_positions": args.learned_train, "epochs": 4,
-                        "loss_accuracy_per_epoch": hist,
-                        "setup_s": time.perf_counter() - t0, "min_empties": 14}
+        learned_info = {"weights": os.path.relpath(args.weights, ROOT), "min_empties": 14}
     tuned, tuned_src = {}, None
     if args.tuned:
         from gpuothello2_gb300 import autotune
@@ -277,14 +295,13 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
 
+    def batched_options():
+        return g.options(method=g.METHOD_BATCHED, use_learned=1 if args.learned else 0,
+                         table_bits=args.table_bits, **tuned)
+
     def solve_device(method):
         st = g.Stats()
-        batched = method == g.METHOD_BATCHED
-        opt = g.options(method=method, split_min_empties=args.split,
-                        use_learned=1 if args.learned and batched else 0,
-                        use_table=1 if args.table and batched else 0,
-                        expand_windows=args.windows if batched else 0,
-                        **(tuned if batched else {}))
+        opt = batched_options() if method == g.METHOD_BATCHED else g.options(method=method)
         rc = L.solve_batch_device(dp.data_ptr(), do.data_ptr(), n, DEPTH, ds.data_ptr(), None,
                                   None, ctypes.byref(opt), ctypes.byref(st), stream.cuda_stream)
         if rc != 0:
@@ -300,9 +317,7 @@ def main():
     def solve_host():
         """One step through the host-buffer entry point (pinned buffers):
         host->device copies, solve, device->host scores, wall clock."""
-        opt = g.options(method=g.METHOD_BATCHED, split_min_empties=args.split,
-                        use_learned=1 if args.learned else 0, use_table=1 if args.table else 0,
-                        expand_windows=args.windows, **tuned)
+        opt = batched_options()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         rc = L.solve_batch_ex(hp.data_ptr(), ho.data_ptr(), n, DEPTH, hs.data_ptr(), None, None,
@@ -323,56 +338,48 @@ def main():
                 solve_device(method)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(steps)]
-        kern_ms, nodes, splits, launches, table = [], [], [], [], []
+        stats = []
         barrier()
         if sampler:
             sampler.__enter__()
         for k in range(steps):
             flush.zero_()
             ev[k][0].record(stream)
-            st = solve_device(method)
+            stats.append(solve_device(method))
             ev[k][1].record(stream)
-            kern_ms.append(st.kernel_ms)
-            nodes.append(st.nodes)
-            splits.append(st.splits)
-            launches.append(st.launches)
-            table.append((st.table_probes, st.table_hits, st.table_updates))
         barrier()
         if sampler:
             sampler.__exit__(None, None, None)
         step_ms = [a.elapsed_time(b) for a, b in ev]
-        timed.splits = splits
-        timed.launches = launches
-        timed.table = table
-        return step_ms, kern_ms, nodes
+        return step_ms, stats
 
     sampler = ClockSampler(local)
     e2e_t = []
-    step_ms, kern_ms, nodes = timed(g.METHOD_BATCHED, args.warmup, args.steps, sampler, e2e_t)
-    batched_splits, batched_launches = list(timed.splits), int(sum(timed.launches))
-    table_stats = None
-    if args.table:
-        probes = sum(t[0] for t in timed.table)
-        hits = sum(t[1] for t in timed.table)
-        updates = sum(t[2] for t in timed.table)
-        kern_s = sum(kern_ms) / 1000.0
-        # each probe reads and each update writes one 16-byte entry: 32-byte
-        # DRAM sectors either way
-        table_stats = {"probes": probes, "hits": hits, "updates": updates,
-                       "sector_bytes": 32 * (probes + updates),
-                       "gbs": 32 * (probes + updates) / kern_s / 1e9 if kern_s > 0 else None}
+    step_ms, stats = timed(g.METHOD_BATCHED, args.warmup, args.steps, sampler, e2e_t)
+    kern_ms = [st.kernel_ms for st in stats]
+    nodes = [st.nodes for st in stats]
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world, dev)
     value = job_value(world, n, args.steps, total_s)
     scores = ds.cpu().numpy()
     e2e_value = job_value(world, n, 1, max_over_ranks(e2e_t[0], world, dev)) if e2e_t else None
     if e2e_t:
         assert np.array_equal(hs.numpy(), scores), "host and device entry points disagree"
+    kern_s = sum(kern_ms) / 1000.0
+    probes = sum(st.table_probes for st in stats)
+    updates = sum(st.table_updates for st in stats)
+    # a probe reads the two 16-byte entries of a bucket (one 32-byte sector);
+    # an update reads the bucket and writes one entry
+    table_stats = {"entries": 1 << int(stats[0].table_bits), "probes": probes,
+                   "hits": sum(st.table_hits for st in stats), "updates": updates,
+                   "sector_bytes": 32 * (probes + 2 * updates),
+                   "gbs": 32 * (probes + 2 * updates) / kern_s / 1e9 if kern_s > 0 else None,
+                   "min_empties": 7}
 
     plain = None
     if args.plain:
-        p_ms, p_kern, p_nodes = timed(g.METHOD_PLAIN, 1, 1)
+        p_ms, p_stats = timed(g.METHOD_PLAIN, 1, 1)
         plain = {"value": n / (p_ms[0] / 1000.0), "unit": "positions/s", "ms_per_step": p_ms[0],
-                 "nodes_per_step": p_nodes[0], "kernel_ms": p_kern[0]}
+                 "nodes_per_step": p_stats[0].nodes, "kernel_ms": p_stats[0].kernel_ms}
         assert np.array_equal(ds.cpu().numpy(), scores), "plain and batched kernels disagree"
 
     peak = ctypes.c_double(0.0)
@@ -388,25 +395,33 @@ def main():
     mean_nodes = statistics.mean(nodes)
     achieved = mean_nodes * W_NODE / mean_kern_s
 
+    parity = None
     cpu = None
-    if rank == 0 and not args.no_cpu:
-        r, done, dt, thr = cpu_reference_rate(CPU_SAMPLE)
-        cpu = {"value": r, "unit": "positions/s", "cores": thr, "kind": "port",
-               "sample": "first %d positions of the workload stream (%.1f s), oracle "
-                         "restatement of the reference tree, %d threads" % (done, dt, thr)}
+    if rank == 0:
+        pos_p = dp.cpu().numpy().view(np.uint64)
+        pos_o = do.cpu().numpy().view(np.uint64)
+        if not args.no_parity:
+            parity = parity_sample(pos_p, pos_o, scores)
+        if not args.no_cpu:
+            r, done, dt, thr = cpu_reference_rate(CPU_SAMPLE)
+            cpu = {"value": r, "unit": "positions/s", "cores": thr, "kind": "port",
+                   "sample": "first %d positions of the workload stream (%.1f s), oracle "
+                             "restatement of the reference tree, %d threads" % (done, dt, thr)}
 
+    launches = int(sum(st.launches for st in stats))
     line = {
         "metric": METRIC, "value": value, "unit": "positions/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic: seeded random playouts (xoshiro256**, seed 2), generated on device",
         "config": {"workload": WORKLOAD, "positions_per_gpu": n, "depth": DEPTH,
-                   "l2": "flushed between steps (256 MiB write, untimed)",
-                   "method": ("batched: empties-bucketed persistent queue, hard positions "
-                              "expanded level by level; learned root ordering %s" %
-                              ("on (--learned)" if args.learned else "off (--learned turns it on)"))
-                   + ("; children of hard positions searched principal variation first "
-                      "(--windows %d)" % args.windows if args.windows else ""),
+                   "l2": "flushed between steps (256 MiB write, untimed); the table clear "
+                         "(16 B x entries) at the start of every solve also evicts it",
+                   "method": ("batched: empties-bucketed persistent queue, per-lane "
+                              "principal-variation search with transposition table and "
+                              "stability cutoff, warp-local helping on hard positions; learned "
+                              "ordering %s" % ("on" if args.learned else "off")),
+                   "table_entries": table_stats["entries"],
                    "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None),
                    "learned": learned_info},
         "e2e": {"value": e2e_value, "unit": "positions/s", "h2d_bytes_per_step": 16 * n,
@@ -414,20 +429,20 @@ def main():
                 "how": "last warm-up step through solve_batch_ex, pinned host buffers, wall clock"},
         "roofline": {"bound": "int32-alu", "achieved": achieved / 1e12, "peak": int_peak / 1e12,
                      "unit": "TOPS (INT32)", "frac": achieved / int_peak,
-                     "traffic": DRAM_BYTES_PER_POSITION * n,
-                     "traffic_source": "ncu capture of 131,072 positions scaled by positions",
+                     "traffic": TRAFFIC_BYTES_PER_NODE * mean_nodes,
+                     "traffic_source": TRAFFIC_SOURCE,
                      "peak_source": "measured live: lop3.b32/add.u32 issue rate (libgpo_intpeak)",
                      "kernel": "batched_kernel", "ops_per_node": W_NODE,
                      "nodes_per_launch": mean_nodes, "kernel_ms": 1000.0 * mean_kern_s},
         "nodes_per_s": mean_nodes / mean_kern_s,
         "nodes_per_position": mean_nodes / n,
-        "splits_per_step": statistics.mean(batched_splits) if batched_splits else 0,
+        "splits_per_step": statistics.mean(st.splits for st in stats),
         "table": table_stats,
+        "parity_sample": parity,
         "cpu_baseline": cpu,
         "clocks": sampler.summary(),
-        # counted by the library per call: bucketing (3) and the search per
-        # pass, plus marking, expansion and combination kernels per level
-        "gpu_launches": batched_launches,
+        # counted by the library per call: bucketing (3) and the search (1)
+        "gpu_launches": launches,
         "plain": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
     }

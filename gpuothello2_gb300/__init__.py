@@ -67,6 +67,7 @@ class Stats(ctypes.Structure):
         ("total_ms", ctypes.c_double),
         ("launches", ctypes.c_uint64),
         ("stability_cuts", ctypes.c_uint64),
+        ("table_bits", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -23,6 +23,7 @@ namespace {
 struct Context {
   int device = -1;
   int sms = 0;
+  size_t mem = 0;  // device memory in bytes
   char name[256] = {0};
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -107,6 +108,7 @@ int ensure_context(Context** out) {
     Context* c = new Context();
     c->device = dev;
     c->sms = prop.multiProcessorCount;
+    c->mem = prop.totalGlobalMem;
     std::snprintf(c->name, sizeof(c->name), "%s", prop.name);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
@@ -183,7 +185,14 @@ int check_options(const gpo_options* opt) {
 // empties when alpha >= 30, helping from 7.
 constexpr int kDefaultFF = 6;
 constexpr int kDefaultTableMin = 7;
-constexpr int kDefaultTableBits = 24;
+// Table size: tens of thousands of searches run at once and share it, so
+// it pays to give it real capacity: 2^28 entries (4 GiB) on a device with
+// at least 64 GiB, else 2^24 (256 MiB).
+constexpr int kDefaultTableBitsLarge = 28;
+constexpr int kDefaultTableBitsSmall = 24;
+int default_table_bits(const Context* c) {
+  return c->mem >= (static_cast<size_t>(64) << 30) ? kDefaultTableBitsLarge : kDefaultTableBitsSmall;
+}
 constexpr int kDefaultStabMin = 6;
 constexpr int kDefaultStabGate = 30;
 constexpr int kDefaultHelpMin = 7;
@@ -266,7 +275,7 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   }
   a.gframes = c->dFrames;
   if (o.use_table != 0) {
-    const int bits = o.table_bits > 0 ? o.table_bits : kDefaultTableBits;
+    const int bits = o.table_bits > 0 ? o.table_bits : default_table_bits(c);
     const int rct = ensure_table(c, bits);
     if (rct != GPO_OK) return rct;
     // cleared at every call: no result carries over from an earlier call
@@ -293,6 +302,7 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
     stats->learned_calls = static_cast<uint64_t>(learned_count);
     stats->splits = hs.handouts;
     stats->stability_cuts = hs.stab_cuts;
+    stats->table_bits = a.tt ? a.tt_bits : 0;
     stats->kernel_ms = ms;
   }
   return status_to_error(hs.status);

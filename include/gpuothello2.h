@@ -69,7 +69,8 @@ typedef struct gpo_options {
                                  the node's first move); 0 = default (7), negative = off */
   int wait_limit_ms;          /* deadline of one search launch; 0 = 600000 */
   int table_bits;             /* transposition table of 2^table_bits 16-byte entries in
-                                 buckets of two (17..32); 0 = 24 */
+                                 buckets of two (17..32); 0 = 28 (4 GiB) on a device with
+                                 >= 64 GiB of memory, else 24 (256 MiB) */
   int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 7 */
   int smem_frames;            /* search frames (depth - 2 slots per lane) in shared memory:
                                  0 = when they all fit at the register-limited occupancy,
@@ -93,6 +94,7 @@ typedef struct gpo_stats {
   double total_ms;         /* wall time of the call */
   uint64_t launches;       /* kernels the call launched */
   uint64_t stability_cuts; /* nodes closed by the stability cutoff */
+  uint64_t table_bits;     /* log2 of the table's entries used by the call (0 = no table) */
 } gpo_stats;
 
 /* Fills *opt with the defaults (all fields "auto"/0). */

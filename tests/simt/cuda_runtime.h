@@ -4,8 +4,7 @@
 // calling thread (work runs when it is enqueued), events read the steady
 // clock, and the emulated device has one SM.  Kernel launches written
 // `k<<<grid, block, smem, stream>>>(args)` are rewritten to simt_launch()
-// when the emulation build copies a source; the one cooperative launch goes
-// through a hook that the emulation sets.
+// when the emulation build copies a source.
 #pragma once
 #include <chrono>
 #include <cstddef>
@@ -16,7 +15,6 @@ typedef int cudaError_t;
 static const cudaError_t cudaSuccess = 0;
 static const cudaError_t cudaErrorInvalidConfiguration = 9;
 static const cudaError_t cudaErrorMemoryAllocation = 2;
-static const cudaError_t cudaErrorNotSupported = 801;
 
 struct SimtStream {
   int unused;
@@ -49,6 +47,7 @@ struct dim3 {
 struct cudaDeviceProp {
   char name[256];
   int multiProcessorCount;
+  size_t totalGlobalMem;
 };
 
 // ---- memory: host memory, filled with a pattern so that a read of memory
@@ -139,14 +138,3 @@ inline cudaError_t cudaOccupancyMaxActiveBlocksPerMultiprocessor(int* n, F, int,
 inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 inline const char* cudaGetErrorName(cudaError_t) { return "simtError"; }
 inline const char* cudaGetErrorString(cudaError_t) { return "error in the SIMT emulation"; }
-
-// ---- the cooperative launch (set by the emulation that links the kernel) ----
-typedef cudaError_t (*SimtCoopLaunch)(const void* f, dim3 grid, dim3 block, void** args);
-inline SimtCoopLaunch& simt_coop_hook() {
-  static SimtCoopLaunch h = nullptr;
-  return h;
-}
-inline cudaError_t cudaLaunchCooperativeKernel(const void* f, dim3 grid, dim3 block, void** args,
-                                               size_t, cudaStream_t) {
-  return simt_coop_hook() ? simt_coop_hook()(f, grid, block, args) : cudaErrorNotSupported;
-}

@@ -79,10 +79,10 @@ def test_learned_root_order_keeps_scores_exact(gpu):
     p, o, best = labelled(gpu, 3, 32768, 12, 14)
     w, _ = gpu.mlp_train(p, o, best, gpu.mlp_init(5), epochs=3, batch=2048, lr=1e-3, seed=2)
     q, r = gpu.generate(4, 2048, 14, 16)
-    s0, _, _, st0, _ = gpu.solve(q, r, 16, use_learned=0, split_min_empties=-1)
+    s0, _, _, st0, _ = gpu.solve(q, r, 16, use_learned=0, help_min_empties=-1)
     gpu.mlp_load(w)
     try:
-        s1, _, _, st1, _ = gpu.solve(q, r, 16, use_learned=1, split_min_empties=-1)
+        s1, _, _, st1, _ = gpu.solve(q, r, 16, use_learned=1, help_min_empties=-1)
     finally:
         gpu.mlp_load(None)
     assert np.array_equal(s0, s1)

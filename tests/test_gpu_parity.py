@@ -37,29 +37,12 @@ def test_gpu_generator_matches_oracle_stream(gpu, oracle):
 def test_scores_match_reference(gpu, name, seed, count, lo, hi, depth, method):
     if method == PLAIN and depth > 16:
         pytest.skip("one thread per position in the reference tree: minutes at 18-22 empties")
-    if depth > 18:
-        pytest.skip("4 positions of 20-22 empties take longer than a test run on this engine")
     p, o, scores, _ = golden_ref(name)
-    sc, _, _, st, _ = gpu.solve(p, o, depth, method=method, wait_limit_ms=60000)
+    sc, _, _, st, _ = gpu.solve(p, o, depth, method=method, wait_limit_ms=300000)
     assert np.array_equal(sc.astype(int), scores)
     assert st.nodes > 0
-    # plain: the search kernel; batched: bucketing (3) + search, per pass
-    if method == PLAIN:
-        assert st.launches == 1
-    else:
-        assert st.launches >= 4
-
-
-def test_expansion_levels_larger_than_the_input(gpu):
-    """A small node budget turns 40 positions into thousands of children over
-    several levels: every pass sizes its scratch for its own positions."""
-    p, o, scores, _ = golden_ref("c3_seed2_mixed")
-    small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 11
-    p, o, scores = p[small][:40], o[small][:40], scores[small][:40]
-    sc, best, _, st, _ = gpu.solve(p, o, 16, best=True, expand_budget=2000)
-    assert np.array_equal(sc.astype(int), scores)
-    assert st.splits > 1024
-    assert ((best >= 0) & (best <= 64)).all()
+    # plain: the search kernel; batched: bucketing (3) + the search
+    assert st.launches == (1 if method == PLAIN else 4)
 
 
 @pytest.mark.parametrize("name,depth", [("c1_seed0_e10", 10), ("c3_seed2_mixed", 16),
@@ -202,33 +185,51 @@ def test_cli_output_matches_reference_file(gpu, tmp_path):
         assert [ln.split() for ln in open(out)] == ref
 
 
-@pytest.mark.parametrize("name,depth,split", [("c4_seed4_e18", 18, 10), ("c4_seed4_e18", 18, 13),
-                                              ("c3_seed2_mixed", 16, 6), ("c3_seed2_mixed", 16, 12),
-                                              ("c3_seed2_mixed", 16, -1)])
-def test_split_search_is_exact(gpu, name, depth, split):
-    """Few deep positions: idle lanes take handed-out subtrees (split > 0) or
-    not (split < 0); scores stay exact either way and every position's node
-    count adds up to the launch total."""
+@pytest.mark.parametrize("name,depth,help_min,rpw", [("c4_seed4_e18", 18, 10, 1),
+                                                     ("c3_seed2_mixed", 16, 6, 2),
+                                                     ("c3_seed2_mixed", 16, -1, 0),
+                                                     ("c1_seed0_e10", 10, 5, 1)])
+def test_helping_is_exact(gpu, oracle, name, depth, help_min, rpw):
+    """Few positions per warp: idle lanes search moves of their warp's split
+    nodes (help_min > 0) or stay idle (help_min < 0); scores stay exact, best
+    moves optimal, and the positions' node counts add up to the launch
+    total."""
     p, o, scores, _ = golden_ref(name)
-    sc, best, nodes, st, _ = gpu.solve(p, o, depth, best=True, nodes=True, split_min_empties=split,
+    sc, best, nodes, st, _ = gpu.solve(p, o, depth, best=True, nodes=True,
+                                       help_min_empties=help_min, roots_per_warp=rpw,
                                        wait_limit_ms=120000)
     assert np.array_equal(sc.astype(int), scores)
     assert int(nodes.sum()) == st.nodes
-    if split > 0 and depth >= 18:
+    if help_min > 0:
         assert st.splits > 0
+    else:
+        assert st.splits == 0
+    cp, co, want = [], [], []
+    for i in range(0, len(p), max(1, len(p) // 32)):
+        b = int(best[i])
+        if b >= 64:
+            continue
+        f = oracle.L.orc_flip(int(p[i]), int(o[i]), b)
+        cp.append(int(o[i]) ^ f)
+        co.append(int(p[i]) ^ f ^ (1 << b))
+        want.append(-int(sc[i]))
+    csc, _, _, _ = oracle.solve_batch(np.array(cp, np.uint64), np.array(co, np.uint64), 32, mode=1)
+    assert np.array_equal(csc.astype(int), np.array(want))
 
 
-@pytest.mark.parametrize("name,depth,split", [("c3_seed2_mixed", 16, -1), ("c3_seed2_mixed", 16, 12),
-                                              ("c4_seed4_e18", 18, 10), ("c1_seed0_e10", 10, -1)])
-def test_transposition_table_is_exact(gpu, name, depth, split):
-    """The 128-bit-CAS table (on at nodes with >= 9 empties here) changes
-    node counts only; shared by the lanes that split a position."""
+@pytest.mark.parametrize("name,depth,bits,tmin", [("c3_seed2_mixed", 16, 20, 9),
+                                                  ("c3_seed2_mixed", 16, 17, 5),
+                                                  ("c4_seed4_e18", 18, 24, 7),
+                                                  ("c1_seed0_e10", 10, 20, 4)])
+def test_transposition_table_is_exact(gpu, name, depth, bits, tmin):
+    """The 128-bit-CAS table changes node counts only, whatever its size
+    and threshold (a small table forces constant eviction)."""
     p, o, scores, _ = golden_ref(name)
-    sc, _, _, st, _ = gpu.solve(p, o, depth, use_table=1, table_min_empties=9, table_bits=20,
-                                split_min_empties=split, wait_limit_ms=120000)
+    sc, _, _, st, _ = gpu.solve(p, o, depth, use_table=1, table_min_empties=tmin,
+                                table_bits=bits, wait_limit_ms=120000)
     assert np.array_equal(sc.astype(int), scores)
     assert st.table_probes > 0 and st.table_updates > 0
-    assert st.table_hits <= st.table_probes
+    assert st.table_hits <= st.table_probes and st.table_bits == bits
 
 
 def test_table_options_are_checked(gpu):
