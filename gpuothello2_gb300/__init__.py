@@ -52,6 +52,7 @@ class Options(ctypes.Structure):
         ("smem_frames", ctypes.c_int),
         ("stability_min_empties", ctypes.c_int),
         ("roots_per_warp", ctypes.c_int),
+        ("root_split_plies", ctypes.c_int),
     ]
 
 
@@ -68,6 +69,7 @@ class Stats(ctypes.Structure):
         ("launches", ctypes.c_uint64),
         ("stability_cuts", ctypes.c_uint64),
         ("table_bits", ctypes.c_uint64),
+        ("root_split_positions", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -308,6 +308,196 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   return status_to_error(hs.status);
 }
 
+// ---- small batches: split at the root ----
+// A batch with fewer positions than a fraction of the GPU's warps leaves most
+// of the GPU idle however well each warp searches.  Such a batch is expanded
+// on the host a few plies deep (at most a few hundred positions, so this is
+// bookkeeping, not search); every frontier position is solved exactly by the
+// batched kernel in one launch, and the values are taken back up by negamax.
+// Solving every frontier position with a full window does more work than
+// principal-variation search would, but it spreads a deep position over
+// thousands of lanes.
+
+u64 host_mobility(u64 P, u64 O) {
+  u64 moves = 0;
+  const u64 empty = ~(P | O);
+  const int dr[8] = {0, 0, 1, -1, 1, 1, -1, -1}, dc[8] = {1, -1, 0, 0, 1, -1, 1, -1};
+  for (int sq = 0; sq < 64; ++sq) {
+    if (!((empty >> sq) & 1)) continue;
+    for (int d = 0; d < 8; ++d) {
+      int r = sq / 8 + dr[d], c = sq % 8 + dc[d], run = 0;
+      while (r >= 0 && r < 8 && c >= 0 && c < 8 && ((O >> (r * 8 + c)) & 1)) {
+        r += dr[d];
+        c += dc[d];
+        ++run;
+      }
+      if (run && r >= 0 && r < 8 && c >= 0 && c < 8 && ((P >> (r * 8 + c)) & 1)) {
+        moves |= 1ULL << sq;
+        break;
+      }
+    }
+  }
+  return moves;
+}
+
+u64 host_flip(u64 P, u64 O, int sq) {
+  u64 flips = 0;
+  const int dr[8] = {0, 0, 1, -1, 1, 1, -1, -1}, dc[8] = {1, -1, 0, 0, 1, -1, 1, -1};
+  for (int d = 0; d < 8; ++d) {
+    u64 run = 0;
+    int r = sq / 8 + dr[d], c = sq % 8 + dc[d];
+    while (r >= 0 && r < 8 && c >= 0 && c < 8 && ((O >> (r * 8 + c)) & 1)) {
+      run |= 1ULL << (r * 8 + c);
+      r += dr[d];
+      c += dc[d];
+    }
+    if (r >= 0 && r < 8 && c >= 0 && c < 8 && ((P >> (r * 8 + c)) & 1)) flips |= run;
+  }
+  return flips;
+}
+
+int host_final(u64 P, u64 O) {
+  const int pc = __builtin_popcountll(P), oc = __builtin_popcountll(O);
+  return pc == oc ? 0 : (pc > oc ? 64 - 2 * oc : 2 * pc - 64);
+}
+
+struct SplitNode {
+  u64 P, O;
+  int parent;  // -1 for an input position
+  int move;    // move from the parent (GPO_MOVE_PASS for a pass)
+  int first;   // children [first, first + count), or count = 0 with a value
+  int count;
+  int leaf;    // index in the GPU batch, or -1
+  int value;   // exact value once known
+  unsigned long long nodes;
+};
+
+// Positions per warp below which a batch is split at the root, and the
+// frontier size (in warps) that is enough.
+constexpr int kSplitBelowWarpsDiv = 8;
+
+int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+                   signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
+                   cudaStream_t s, gpo_stats* stats, long warps, int plies_opt) {
+  std::vector<u64> hp(n), ho(n);
+  GPO_CK(cudaMemcpyAsync(hp.data(), dP, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaMemcpyAsync(ho.data(), dO, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  std::vector<SplitNode> t;
+  t.reserve(static_cast<size_t>(n) * 64);
+  for (int i = 0; i < n; ++i) {
+    if ((hp[i] & ho[i]) || 64 - __builtin_popcountll(hp[i] | ho[i]) > depth) return 1;  // not split
+    t.push_back(SplitNode{hp[i], ho[i], -1, kMoveNoneDev, 0, 0, -1, 0, 0});
+  }
+  // expand ply by ply until the frontier has enough positions
+  size_t lo = 0, hi = t.size();
+  const int max_plies = plies_opt > 0 ? plies_opt : 3;
+  for (int ply = 0; ply < max_plies; ++ply) {
+    if (plies_opt <= 0 && static_cast<long>(hi - lo) * kSplitBelowWarpsDiv >= warps * 4) break;
+    for (size_t k = lo; k < hi; ++k) {
+      const u64 P = t[k].P, O = t[k].O;  // copies: push_back below may move t
+      if (64 - __builtin_popcountll(P | O) <= 12) continue;  // small enough to solve whole
+      u64 moves = host_mobility(P, O);
+      const int first = static_cast<int>(t.size());
+      if (moves) {
+        int cnt = 0;
+        while (moves) {
+          const int sq = __builtin_ctzll(moves);
+          moves &= moves - 1;
+          const u64 f = host_flip(P, O, sq);
+          t.push_back(SplitNode{O ^ f, P ^ f ^ (1ULL << sq), static_cast<int>(k), sq, 0, 0, -1, 0, 0});
+          ++cnt;
+        }
+        t[k].first = first;
+        t[k].count = cnt;
+      } else if (host_mobility(O, P)) {
+        t.push_back(SplitNode{O, P, static_cast<int>(k), kMovePassDev, 0, 0, -1, 0, 0});
+        t[k].first = first;
+        t[k].count = 1;
+      } else {
+        t[k].value = host_final(P, O);  // game over: count stays 0, no leaf
+        t[k].leaf = -2;
+      }
+    }
+    lo = hi;
+    hi = t.size();
+  }
+  // frontier positions (no children, value unknown) go to the GPU
+  std::vector<u64> lp, lo_;
+  for (size_t k = 0; k < t.size(); ++k) {
+    if (t[k].count == 0 && t[k].leaf != -2) {
+      t[k].leaf = static_cast<int>(lp.size());
+      lp.push_back(t[k].P);
+      lo_.push_back(t[k].O);
+    }
+  }
+  const int m = static_cast<int>(lp.size());
+  std::vector<signed char> lsc(m), lbest(m, kMoveNoneDev);
+  std::vector<unsigned long long> lnodes(m, 0);
+  gpo_stats inner;
+  std::memset(&inner, 0, sizeof(inner));
+  if (m > 0) {
+    // the outputs may be the context's own staging buffers (host-buffer entry
+    // point), which growing them replaces
+    const bool staged = dScore == c->dScore;
+    int rc = ensure_capacity(c, static_cast<size_t>(m));
+    if (rc != GPO_OK) return rc;
+    if (staged) {
+      dScore = c->dScore;
+      if (dBest) dBest = c->dBest;
+      if (dNodes) dNodes = c->dNodes;
+    }
+    GPO_CK(cudaMemcpyAsync(c->dP, lp.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
+    GPO_CK(cudaMemcpyAsync(c->dO, lo_.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
+    rc = run_batched(c, c->dP, c->dO, m, depth, c->dScore, dBest ? c->dBest : nullptr,
+                     dNodes ? c->dNodes : nullptr, o, s, &inner);
+    if (rc != GPO_OK) return rc;
+    GPO_CK(cudaMemcpyAsync(lsc.data(), c->dScore, m, cudaMemcpyDeviceToHost, s));
+    if (dBest) GPO_CK(cudaMemcpyAsync(lbest.data(), c->dBest, m, cudaMemcpyDeviceToHost, s));
+    if (dNodes)
+      GPO_CK(cudaMemcpyAsync(lnodes.data(), c->dNodes, m * sizeof(u64), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaStreamSynchronize(s));
+  }
+  // negamax from the deepest nodes up (children come after their parents)
+  std::vector<int> bestmove(t.size(), kMoveNoneDev);
+  for (size_t k = t.size(); k-- > 0;) {
+    SplitNode& nd = t[k];
+    nd.nodes += 1;
+    if (nd.leaf >= 0) {
+      nd.value = lsc[nd.leaf];
+      nd.nodes = lnodes[nd.leaf];
+      bestmove[k] = lbest[nd.leaf];  // used where an input position was not expanded
+    } else if (nd.count > 0) {
+      int best = -65;
+      for (int j = nd.first; j < nd.first + nd.count; ++j) {
+        nd.nodes += t[j].nodes;
+        if (-t[j].value > best) {
+          best = -t[j].value;
+          bestmove[k] = t[j].move;
+        }
+      }
+      nd.value = best;
+    }
+  }
+  std::vector<signed char> sc(n), bm(n);
+  std::vector<unsigned long long> nds(n);
+  for (int i = 0; i < n; ++i) {
+    sc[i] = static_cast<signed char>(t[i].value);
+    bm[i] = static_cast<signed char>(bestmove[i]);
+    nds[i] = t[i].nodes;
+  }
+  GPO_CK(cudaMemcpyAsync(dScore, sc.data(), n, cudaMemcpyHostToDevice, s));
+  if (dBest) GPO_CK(cudaMemcpyAsync(dBest, bm.data(), n, cudaMemcpyHostToDevice, s));
+  if (dNodes) GPO_CK(cudaMemcpyAsync(dNodes, nds.data(), n * sizeof(u64), cudaMemcpyHostToDevice, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  if (stats) {
+    *stats = inner;
+    stats->nodes = inner.nodes + (t.size() - static_cast<size_t>(m));
+    stats->root_split_positions = static_cast<uint64_t>(m);
+  }
+  return GPO_OK;
+}
+
 // Runs the solve pipeline on device arrays already in place.
 int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
               signed char* dBest, unsigned long long* dNodes, const gpo_options* opt,
@@ -331,6 +521,19 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
       stats->kernel_ms = ms;
     }
     return status_to_error(hs.status);
+  }
+  // a batch far too small to give every warp a position is split at the root
+  if (o.root_split_plies >= 0 && depth >= 14) {
+    int threads = o.threads_per_block > 0 ? o.threads_per_block : 128, top = 2, grid = 0;
+    size_t smem = 0;
+    GPO_CK(batched_plan(threads, depth, &top));
+    GPO_CK(batched_grid(threads, top, c->sms, &grid, &smem));
+    const long warps = static_cast<long>(grid) * (threads / 32);
+    if (o.root_split_plies > 0 || static_cast<long>(n) * kSplitBelowWarpsDiv < warps) {
+      const int rc = run_root_split(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, warps,
+                                    o.root_split_plies);
+      if (rc != 1) return rc;  // 1: inputs the kernel must reject, solved unsplit below
+    }
   }
   return run_batched(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats);
 }

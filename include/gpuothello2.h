@@ -81,6 +81,12 @@ typedef struct gpo_options {
   int roots_per_warp;         /* input positions a warp searches at once, the rest of its
                                  lanes helping (1..32); 0 = from the batch size: 32 when the
                                  batch fills the GPU, fewer for small batches */
+  int root_split_plies;       /* batches with fewer positions than 1/8 of the GPU's warps
+                                 (depth >= 14): 0 = expanded on the host until the frontier
+                                 fills the GPU (at most 3 plies; positions with <= 12 empties
+                                 are not expanded), every frontier position solved exactly in
+                                 one launch, values taken back up by negamax; > 0 = always
+                                 expand this many plies; negative = never */
 } gpo_options;
 
 typedef struct gpo_stats {
@@ -95,6 +101,7 @@ typedef struct gpo_stats {
   uint64_t launches;       /* kernels the call launched */
   uint64_t stability_cuts; /* nodes closed by the stability cutoff */
   uint64_t table_bits;     /* log2 of the table's entries used by the call (0 = no table) */
+  uint64_t root_split_positions; /* frontier positions a root split solved (0 = no split) */
 } gpo_stats;
 
 /* Fills *opt with the defaults (all fields "auto"/0). */

@@ -90,6 +90,24 @@ def test_helping_on_few_positions(emu, oracle):
     best_moves_reach_scores(oracle, p, o, sc, bm)
 
 
+@pytest.mark.parametrize("plies", [1, 2])
+def test_root_split_of_small_batches(emu, oracle, plies):
+    """A small batch expanded at the root on the host: every frontier
+    position solved by the kernel, values taken back up by negamax; scores,
+    best moves (including passes) and node totals as the unsplit solve."""
+    p, o = oracle.generate(13, 5, 13, 14)
+    p = np.concatenate([p, [np.uint64(0xFFFFFFFF00000000)]])  # a finished game (0 empties)
+    o = np.concatenate([o, [np.uint64(0x00000000FFFFFFFF)]])
+    want, _, _, _ = oracle.solve_batch(p, o, mode=1)
+    rc, sc, bm, nodes, st = solve(emu, p, o, 14, root_split_plies=plies)
+    assert rc == 0 and np.array_equal(sc, want)
+    assert st.root_split_positions > len(p) and st.nodes == int(nodes.sum())
+    best_moves_reach_scores(oracle, p[:-1], o[:-1], sc[:-1], bm[:-1])
+    assert int(bm[-1]) == g.MOVE_NONE
+    rc, sc2, _, _, st2 = solve(emu, p, o, 14, root_split_plies=-1)
+    assert rc == 0 and np.array_equal(sc2, want) and st2.root_split_positions == 0
+
+
 def test_mixed_empties_without_shared_frames(emu):
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
     small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 11
