@@ -38,7 +38,7 @@ def test_scores_match_reference(gpu, name, seed, count, lo, hi, depth, method):
     if method == PLAIN and depth > 16:
         pytest.skip("one thread per position in the reference tree: minutes at 18-22 empties")
     p, o, scores, _ = golden_ref(name)
-    sc, _, _, st, _ = gpu.solve(p, o, depth, method=method, wait_limit_ms=300000)
+    sc, _, _, st, _ = gpu.solve(p, o, depth, method=method, wait_limit_ms=600000)
     assert np.array_equal(sc.astype(int), scores)
     assert st.nodes > 0
     # plain: the search kernel; batched: bucketing (3) + the search
