@@ -14,7 +14,7 @@ SPACE = (
     ("threads_per_block", (64, 128, 256)),
     ("smem_frames", (0, -1)),
     ("fastest_first_empties", (5, 6, 9)),
-    ("help_min_empties", (6, -1)),
+    ("help_min_empties", (7, -1)),
 )
 
 

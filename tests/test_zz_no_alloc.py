@@ -24,7 +24,7 @@ def test_noalloc_matches_allocating_entry_point(gpu):
     dp = torch.empty(n, dtype=torch.int64, device="cuda")
     do = torch.empty(n, dtype=torch.int64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
-    assert L.gpo_generate_device(2, 0, n, 8, 16, dp.data_ptr(), do.data_ptr(), stream) == 0
+    assert L.gpo_generate_device(2, 0, n, 8, 13, dp.data_ptr(), do.data_ptr(), stream) == 0
     ref = torch.zeros(n, dtype=torch.int8, device="cuda")
     opt = g.options(use_table=0)
     st = g.Stats()
