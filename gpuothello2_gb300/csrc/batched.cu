@@ -183,6 +183,21 @@ __device__ __forceinline__ int tt_record(unsigned long long* tt, int bits, u64 P
 
 __device__ __noinline__ int stable_count(u64 O, u64 occ) { return popc(gpo_stable(O, occ)); }
 
+// The learned move list of (P, O) from the order table, or 0 (mlp.cu fills
+// the table with linear probing from the key's bucket, at most 16 slots).
+__device__ __noinline__ u64 order_lookup(const u64* table, int bits, u64 P, u64 O) {
+  const TTKey k = tt_key(P, O);
+  const size_t mask = (static_cast<size_t>(1) << bits) - 1;
+  size_t h = static_cast<size_t>(k.y >> (64 - bits));
+  for (int probe = 0; probe < 16; ++probe, h = (h + 1) & mask) {
+    const u64* e = table + 4 * h;
+    const u64 x = e[0], y = e[1];
+    if (x == k.x && y == k.y) return e[2];
+    if ((x | y) == 0) return 0;
+  }
+  return 0;
+}
+
 // A lane's split node: the shallowest of its open nodes (slots root_e down
 // to E + 1) with >= help_min empties that is not passed, has searched its
 // first move, has an open window and has a move left in its frame.  The
@@ -674,12 +689,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
       moves = cm;
       phase = PH_MASK;
       start_keys = (cm & (cm - 1)) && E >= args.ff;
-      if (cm && !helper && E == root_e && best == -65 && args.root_lists &&
-          E >= args.learned_min) {
-        moves = args.root_lists[pos];  // the learned orderer's five best moves
-        phase = PH_LIST;
-        start_keys = false;
-      }
+      created = E == root_e && best == -65 && !helper;  // an input position's first init
     } else if (op == OP_REMASK) {
       moves = cm & ~list_squares(moves);
       phase = PH_MASK;
@@ -728,7 +738,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
         created = true;
       }
     }
-    if (created && !abort) {
+    if (created && !abort && op != OP_INIT) {
       if (args.tt_min && E >= args.tt_min) {
         ++tt_probes;
         const unsigned h = tt_lookup(args.tt, args.tt_bits, P, O);
@@ -763,6 +773,14 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
         // reports the error
         atomicOr(&args.stats->status, kErrBudget);
         abort = true;
+      }
+    }
+    if (created && !closed && args.order_table && E >= args.learned_min && (cm & (cm - 1))) {
+      const u64 l = order_lookup(args.order_table, args.order_bits, P, O);
+      if (l) {  // the learned orderer's five best moves replace the ordering probes
+        moves = l;
+        phase = PH_LIST;
+        start_keys = false;
       }
     }
     if (start_keys) {

@@ -33,9 +33,14 @@ struct Context {
   signed char* dScore = nullptr;
   signed char* dBest = nullptr;
   unsigned long long* dNodes = nullptr;
-  size_t pass_cap = 0;  // per-position scratch of a search: queue order, learned root lists
+  size_t pass_cap = 0;  // per-position scratch of a search: queue order
   unsigned* dPerm = nullptr;
-  u64* dLists = nullptr;
+  long front_cap = 0;   // learned ordering: frontier positions and the order table
+  u64* dFrontP = nullptr;
+  u64* dFrontO = nullptr;
+  u64* dOrder = nullptr;
+  int order_bits = 0;
+  unsigned long long* dCounter = nullptr;
   unsigned* dHist = nullptr;    // 65 buckets
   unsigned* dCursor = nullptr;  // 65 bucket cursors
   DeviceStats* dStats = nullptr;
@@ -86,7 +91,10 @@ void free_context(Context* c) {
   cudaStreamSynchronize(c->stream);
   free_buffers(c);
   cudaFree(c->dPerm);
-  cudaFree(c->dLists);
+  cudaFree(c->dFrontP);
+  cudaFree(c->dFrontO);
+  cudaFree(c->dOrder);
+  cudaFree(c->dCounter);
   cudaFree(c->dFrames);
   cudaFree(c->dTable);
   cudaFree(c->dHist);
@@ -116,6 +124,7 @@ int ensure_context(Context** out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->dHist, 65 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&c->dCursor, 65 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&c->dStats, sizeof(DeviceStats));
+    if (e == cudaSuccess) e = cudaMalloc(&c->dCounter, sizeof(unsigned long long));
     if (e != cudaSuccess) {
       free_context(c);
       return cuda_fail(e, "context setup");
@@ -140,23 +149,43 @@ int ensure_capacity(Context* c, size_t n) {
   return GPO_OK;
 }
 
-// Per-position scratch of a search (queue order, learned root lists),
-// grown on demand and kept by the context: repeated calls of the same size
-// allocate nothing.
+// Per-position scratch of a search (queue order), grown on demand and kept
+// by the context: repeated calls of the same size allocate nothing.
 int ensure_pass_scratch(Context* c, size_t n) {
   if (n <= c->pass_cap) return GPO_OK;
   cudaFree(c->dPerm);
-  cudaFree(c->dLists);
   c->dPerm = nullptr;
-  c->dLists = nullptr;
   c->pass_cap = 0;
   size_t cap = 1024;
   while (cap < n) cap *= 2;
   GPO_CK(cudaMalloc(&c->dPerm, cap * sizeof(unsigned)));
-  GPO_CK(cudaMalloc(&c->dLists, cap * sizeof(u64)));
   c->pass_cap = cap;
   return GPO_OK;
 }
+
+// Learned ordering: frontier positions (capacity cap) and an order table of
+// at least twice as many entries, grown on demand.
+int ensure_frontier(Context* c, long cap) {
+  if (cap <= c->front_cap) return GPO_OK;
+  cudaFree(c->dFrontP);
+  cudaFree(c->dFrontO);
+  cudaFree(c->dOrder);
+  c->dFrontP = c->dFrontO = c->dOrder = nullptr;
+  c->front_cap = 0;
+  int bits = 10;
+  while ((1L << bits) < 2 * cap) ++bits;
+  GPO_CK(cudaMalloc(&c->dFrontP, cap * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->dFrontO, cap * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->dOrder, (static_cast<size_t>(32)) << bits));
+  c->order_bits = bits;
+  c->front_cap = cap;
+  return GPO_OK;
+}
+
+// Frontier nodes reserved per deep root: a position with two plies of
+// >= L empties below it has about 70 (1 + ~8 children + ~60 grandchildren);
+// the rare larger ones past the capacity keep the fastest-first order.
+constexpr long kFrontierPerRoot = 96;
 
 int status_to_error(unsigned st) {
   if (st & kErrOverlap) return GPO_ERR_BOARD;
@@ -208,11 +237,12 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   GPO_CK(cudaMemsetAsync(c->dHist, 0, 65 * sizeof(unsigned), s));
   GPO_CK(launch_bucket(dP, dO, n, depth, c->dHist, c->dCursor, c->dPerm, c->dStats, c->sms, s));
   c->launches += 3;
-  // Learned root orders for the positions with >= learned_min empties
-  // (the front of the bucketed queue).
+  // Learned ordering for the positions with >= learned_min empties (the
+  // front of the bucketed queue): the network scores the top two plies of
+  // their trees ahead of the search (mlp_order_frontier).
   const int lmin = o.learned_min_empties > 0 ? o.learned_min_empties : 14;
   const bool learned = (o.use_learned > 0 || (o.use_learned < 0 && mlp_loaded())) && depth >= lmin;
-  long learned_count = 0;
+  long learned_count = 0, frontier = 0;
   if (learned) {
     if (!mlp_loaded()) return GPO_ERR_ARG;
     unsigned hist[65];
@@ -220,8 +250,12 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
     GPO_CK(cudaStreamSynchronize(s));
     for (int e = lmin; e <= 64; ++e) learned_count += hist[e];
     if (learned_count > 0) {
+      const int rcf = ensure_frontier(c, learned_count * kFrontierPerRoot);
+      if (rcf != GPO_OK) return rcf;
       unsigned launched = 0;
-      const int rcl = mlp_order_roots(dP, dO, c->dPerm, learned_count, c->dLists, s, &launched);
+      const int rcl = mlp_order_frontier(dP, dO, c->dPerm, learned_count, lmin, c->dFrontP,
+                                         c->dFrontO, c->front_cap, c->dCounter, c->dOrder,
+                                         c->order_bits, s, &launched, &frontier);
       c->launches += launched;
       if (rcl != GPO_OK) return rcl;
     }
@@ -243,7 +277,8 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   a.help_min = o.help_min_empties > 0 ? o.help_min_empties
                                       : (o.help_min_empties < 0 ? 0 : kDefaultHelpMin);
   a.node_budget = o.node_budget;
-  a.root_lists = learned_count > 0 ? c->dLists : nullptr;
+  a.order_table = frontier > 0 ? c->dOrder : nullptr;
+  a.order_bits = c->order_bits;
   a.learned_min = lmin;
   a.wait_limit_ns =
       static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 600000) * 1000000ULL;
@@ -299,7 +334,7 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
     stats->table_probes = hs.tt_probes;
     stats->table_hits = hs.tt_hits;
     stats->table_updates = hs.tt_updates;
-    stats->learned_calls = static_cast<uint64_t>(learned_count);
+    stats->learned_calls = static_cast<uint64_t>(frontier);
     stats->splits = hs.handouts;
     stats->stability_cuts = hs.stab_cuts;
     stats->table_bits = a.tt ? a.tt_bits : 0;

@@ -41,10 +41,12 @@ struct BatchedArgs {
   unsigned long long* tt;
   int tt_bits;
   int tt_min;
-  // Learned root orders (mlp.cu): for an input position with at least
-  // learned_min empties, root_lists[pos] replaces the root's ordering
-  // probes (null = off).
-  const u64* root_lists;
+  // Learned order table (mlp.cu): 2^order_bits entries of {x, y, list, 0};
+  // a node with at least learned_min empties and two or more moves found
+  // there searches its moves in the listed order instead of fastest-first
+  // (null = off).
+  const u64* order_table;
+  int order_bits;
   int learned_min;
   unsigned long long node_budget;    // per input position, 0 = none (watchdog)
   unsigned long long wait_limit_ns;  // deadline of the launch, from its start
@@ -79,8 +81,14 @@ size_t batched_gframe_bytes(int depth, int smem_top, size_t lanes);
 
 // Learned orderer (mlp.cu).
 bool mlp_loaded();
-// *launched receives the number of kernels it launched.
-int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
-                    u64* d_lists, cudaStream_t s, unsigned* launched);
+// Learned order table for the roots d_idx[0..count) (mlp.cu): frontier of
+// nodes with >= L empties two plies deep, scored by the network, inserted
+// into `table` (2^table_bits entries of 32 bytes, cleared by the call).
+// *launched receives the number of kernels it launched, *frontier the
+// frontier nodes scored.
+int mlp_order_frontier(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
+                       int L, u64* frontP, u64* frontO, long cap, unsigned long long* counter,
+                       u64* table, int table_bits, cudaStream_t s, unsigned* launched,
+                       long* frontier);
 
 }  // namespace gpo

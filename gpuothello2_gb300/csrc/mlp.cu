@@ -9,8 +9,9 @@
 //
 // Labels are the best moves returned by the solver itself (solve_batch_ex's
 // best_move).  The orderer only changes which move is searched first, so
-// scores stay exact; it replaces the fastest-first probes at the roots of
-// positions with >= learned_min_empties empties.
+// scores stay exact; it replaces the fastest-first probes at the nodes with
+// >= learned_min_empties empties in the top two plies of the search (see
+// the learned order table below).
 //
 // Every product (forward, the two input-gradient and three weight-gradient
 // products of backward) is one generic kernel: C = A * B with arbitrary
@@ -30,6 +31,7 @@
 #include "../../include/gpuothello2.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "table.cuh"
 
 namespace gpo {
 
@@ -400,11 +402,97 @@ __global__ void gather_kernel(const u64* __restrict__ P, const u64* __restrict__
   }
 }
 
-__global__ void scatter_lists_kernel(const u64* __restrict__ lists,
-                                     const unsigned* __restrict__ idx, long off, long count,
-                                     int rows, u64* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < rows && off + i < count) out[idx[off + i]] = lists[i];
+// ---- learned order table: move lists for the top of the search ----
+// The search asks for a node's move order when it creates the node, at
+// random moments in 32 independent lanes per warp; a network evaluated then
+// would run one row at a time.  Instead, before the search, every node with
+// >= L empties in the top two plies below each deep root is enumerated (the
+// frontier the search will meet first), the network scores the whole
+// frontier in large batches on the tensor cores, and the resulting lists go
+// into a table keyed exactly by position (the transposition table's
+// bijective key, table.cuh).  Entry: 4 words {x, y, list, 0}; x = y = 0 is
+// empty (no real position maps there).  Linear probing, at most
+// kOrderProbe slots.
+
+// Nodes with >= L empties from the root down two plies (a pass counts as a
+// ply: the swapped position); emit = false only counts them.
+__device__ __forceinline__ int frontier_walk(u64 P, u64 O, int L, const u64* rays, bool emit,
+                                             u64* outP, u64* outO, long at, long cap) {
+  int k = 0;
+  auto put = [&](u64 a, u64 b) {
+    if (emit && at + k < cap) {
+      outP[at + k] = a;
+      outO[at + k] = b;
+    }
+    ++k;
+  };
+  if (64 - popc(P | O) < L) return 0;
+  put(P, O);
+  u64 m1 = gpo_mobility(P, O);
+  const bool pass1 = !m1;
+  if (pass1) m1 = gpo_mobility(O, P) ? 1ULL << 63 : 0ULL;  // one "move": the pass
+  while (m1) {
+    const int s1 = ctz64(m1);
+    m1 &= m1 - 1;
+    u64 cP, cO;
+    if (pass1) {
+      cP = O;
+      cO = P;
+    } else {
+      const u64 f = gpo_flip(P, O, s1, rays);
+      cP = O ^ f;
+      cO = P ^ f ^ (1ULL << s1);
+    }
+    if (64 - popc(cP | cO) < L) continue;
+    put(cP, cO);
+    u64 m2 = gpo_mobility(cP, cO);
+    while (m2) {
+      const int s2 = ctz64(m2);
+      m2 &= m2 - 1;
+      const u64 f = gpo_flip(cP, cO, s2, rays);
+      const u64 gP = cO ^ f, gO = cP ^ f ^ (1ULL << s2);
+      if (64 - popc(gP | gO) >= L) put(gP, gO);
+    }
+  }
+  return k;
+}
+
+__global__ void frontier_kernel(const u64* __restrict__ P, const u64* __restrict__ O,
+                                const unsigned* __restrict__ perm, long count, int L,
+                                u64* __restrict__ outP, u64* __restrict__ outO,
+                                unsigned long long* __restrict__ counter, long cap) {
+  __shared__ __align__(16) u64 rays[256];
+  gpo_build_rays(rays);
+  __syncthreads();
+  const long i = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const unsigned j = perm[i];
+  const u64 p = P[j], o = O[j];
+  const int k = frontier_walk(p, o, L, rays, false, nullptr, nullptr, 0, 0);
+  if (!k) return;
+  const long at = static_cast<long>(atomicAdd(counter, static_cast<unsigned long long>(k)));
+  if (at + k <= cap) frontier_walk(p, o, L, rays, true, outP, outO, at, cap);
+}
+
+constexpr int kOrderProbe = 16;
+
+__global__ void order_insert_kernel(const u64* __restrict__ fP, const u64* __restrict__ fO,
+                                    const u64* __restrict__ lists, long off, long count, int rows,
+                                    u64* __restrict__ table, int bits) {
+  const long r = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= rows || off + r >= count) return;
+  const TTKey k = tt_key(fP[off + r], fO[off + r]);
+  const size_t mask = (static_cast<size_t>(1) << bits) - 1;
+  size_t h = static_cast<size_t>(k.y >> (64 - bits));
+  for (int probe = 0; probe < kOrderProbe; ++probe, h = (h + 1) & mask) {
+    u64 o0, o1;
+    tt_cas128(table + 4 * h, 0, 0, k.x, k.y, o0, o1);
+    if ((o0 | o1) == 0) {  // claimed
+      table[4 * h + 2] = lists[r];
+      return;
+    }
+    if (o0 == k.x && o1 == k.y) return;  // the same position, already there
+  }
 }
 
 Net g_infer;        // network loaded for the solver
@@ -422,25 +510,43 @@ bool mlp_loaded() {
   return g_loaded;
 }
 
-// Root orders for the `count` positions d_idx[0..count) of d_player/d_opp:
-// d_lists[d_idx[i]] = packed list of the five best legal moves by logit.
-int mlp_order_roots(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
-                    u64* d_lists, cudaStream_t s, unsigned* launched) {
+// Learned order table for the search: the frontier of the `count` roots
+// d_idx[0..count) (nodes with >= L empties, top two plies) into
+// frontP/frontO (capacity cap), scored by the network, inserted into the
+// table of 2^table_bits entries (cleared here).  *frontier receives the
+// number of frontier nodes (those past cap are left out: their nodes use
+// the fastest-first order).
+int mlp_order_frontier(const u64* d_player, const u64* d_opp, const unsigned* d_idx, long count,
+                       int L, u64* frontP, u64* frontO, long cap, unsigned long long* counter,
+                       u64* table, int table_bits, cudaStream_t s, unsigned* launched,
+                       long* frontier) {
   *launched = 0;
+  *frontier = 0;
   std::lock_guard<std::mutex> lock(g_mlp_mutex);
   if (!g_loaded) return GPO_ERR_ARG;
   Net& t = g_infer;
-  for (long off = 0; off < count; off += t.rows) {
-    *launched += 6;  // gather, three GEMMs, order, scatter
-    gather_kernel<<<t.rows, 64, 0, s>>>(d_player, d_opp, d_idx, off, count, t.rows, t.X, t.legal,
+  MLP_CK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
+  MLP_CK(cudaMemsetAsync(table, 0, (static_cast<size_t>(32)) << table_bits, s));
+  frontier_kernel<<<static_cast<unsigned>((count + 127) / 128), 128, 0, s>>>(
+      d_player, d_opp, d_idx, count, L, frontP, frontO, counter, cap);
+  MLP_CK(cudaGetLastError());
+  *launched += 1;
+  unsigned long long nf = 0;
+  MLP_CK(cudaMemcpyAsync(&nf, counter, sizeof(nf), cudaMemcpyDeviceToHost, s));
+  MLP_CK(cudaStreamSynchronize(s));
+  const long total = static_cast<long>(nf < static_cast<unsigned long long>(cap) ? nf : cap);
+  for (long off = 0; off < total; off += t.rows) {
+    *launched += 6;  // gather, three GEMMs, order, insert
+    gather_kernel<<<t.rows, 64, 0, s>>>(frontP, frontO, nullptr, off, total, t.rows, t.X, t.legal,
                                          nullptr, nullptr);
     MLP_CK(cudaGetLastError());
     MLP_CK(forward(t, t.rows, s));
     order_kernel<<<(t.rows + 127) / 128, 128, 0, s>>>(t.Z, t.legal, t.rows, g_lists_tmp);
-    scatter_lists_kernel<<<(t.rows + 127) / 128, 128, 0, s>>>(g_lists_tmp, d_idx, off, count,
-                                                               t.rows, d_lists);
+    order_insert_kernel<<<(t.rows + 127) / 128, 128, 0, s>>>(frontP, frontO, g_lists_tmp, off, total,
+                                                              t.rows, table, table_bits);
     MLP_CK(cudaGetLastError());
   }
+  *frontier = total;
   return GPO_OK;
 }
 

@@ -5,7 +5,7 @@
 // emu_batched() runs batched_kernel as one block of `warps` x 32 CPU threads
 // over n positions, with the buffers the C-ABI layer would give it: the
 // empties-descending queue order, the frame placements, the transposition
-// table and learned root lists.  Tests compare its scores with the oracle
+// table and a learned order table.  Tests compare its scores with the oracle
 // and exercise the code paths a GPU run takes (helping between the lanes
 // of a warp, the table, the stability cutoff, node budgets).
 #include <algorithm>
@@ -42,7 +42,8 @@ struct EmuOptions {
   unsigned long long node_budget;   // per position, 0 = none
   int tt_bits;                      // 0 = no table
   int tt_min;
-  const unsigned long long* root_lists;  // learned root orders per position, or null
+  const unsigned long long* order_table;  // learned order table, or null
+  int order_bits;
   int learned_min;
 };
 
@@ -86,7 +87,8 @@ int emu_batched(const unsigned long long* P, const unsigned long long* O, int n,
     a.tt_bits = opt->tt_bits;
     a.tt_min = opt->tt_min > 0 ? opt->tt_min : 7;
   }
-  a.root_lists = opt->root_lists;
+  a.order_table = opt->order_table;
+  a.order_bits = opt->order_bits;
   a.learned_min = opt->learned_min > 0 ? opt->learned_min : 14;
   a.wait_limit_ns = 600ULL * 1000000000ULL;
   const size_t smem = batched_smem_bytes(T, a.smem_top);

@@ -44,9 +44,11 @@ alignas(16) u64 smem_raw[kEmuSmemWords];
 
 // the learned orderer is not part of this build
 bool mlp_loaded() { return false; }
-int mlp_order_roots(const u64*, const u64*, const unsigned*, long, u64*, cudaStream_t,
-                    unsigned* launched) {
+int mlp_order_frontier(const u64*, const u64*, const unsigned*, long, int, u64*, u64*, long,
+                       unsigned long long*, u64*, int, cudaStream_t, unsigned* launched,
+                       long* frontier) {
   *launched = 0;
+  *frontier = 0;
   return GPO_ERR_ARG;
 }
 

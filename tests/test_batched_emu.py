@@ -20,8 +20,8 @@ class EmuOptions(ctypes.Structure):
                 ("help_min", ctypes.c_int), ("roots_per_warp", ctypes.c_int),
                 ("stab_min", ctypes.c_int), ("stab_gate", ctypes.c_int),
                 ("node_budget", ctypes.c_uint64), ("tt_bits", ctypes.c_int),
-                ("tt_min", ctypes.c_int), ("root_lists", ctypes.c_void_p),
-                ("learned_min", ctypes.c_int)]
+                ("tt_min", ctypes.c_int), ("order_table", ctypes.c_void_p),
+                ("order_bits", ctypes.c_int), ("learned_min", ctypes.c_int)]
 
 
 @pytest.fixture(scope="module")
@@ -137,8 +137,8 @@ def test_rejected_inputs(emu, c1):
     assert int(st[6]) & DEPTH
 
 
-def pack_root_list(moves, total):
-    """A root list as the learned orderer writes it (mlp.cu order_kernel):
+def pack_list(moves, total):
+    """A move list as the learned orderer writes it (mlp.cu order_kernel):
     up to five (slot << 6 | square) entries of 12 bits, unused entries all
     ones, bit 63 set when the position has more legal moves than the list."""
     lst = 0x0FFFFFFFFFFFFFFF
@@ -150,23 +150,60 @@ def pack_root_list(moves, total):
     return lst
 
 
+M64 = (1 << 64) - 1
+
+
+def table_key(p, o):
+    """The exact position key of table.cuh (tt_key)."""
+    x = (p * 0x9E3779B97F4A7C15) & M64
+    r = ((x << 32) | (x >> 32)) & M64
+    return x, ((o ^ r) * 0xD6E8FEB86659FD93) & M64
+
+
+def order_table(entries, bits):
+    """The learned order table as mlp.cu builds it: {x, y, list, 0} per
+    entry, linear probing from the high bits of y."""
+    t = np.zeros(4 << bits, np.uint64)
+    for (p, o), lst in entries.items():
+        x, y = table_key(p, o)
+        h = y >> (64 - bits)
+        while t[4 * h] or t[4 * h + 1]:
+            h = (h + 1) & ((1 << bits) - 1)
+        t[4 * h], t[4 * h + 1], t[4 * h + 2] = x, y, lst
+    return t
+
+
 @pytest.mark.parametrize("order", ["high_first", "best_first"])
-def test_learned_root_lists_keep_scores_exact(emu, oracle, c1, order):
+def test_learned_order_table_keeps_scores_exact(emu, oracle, c1, order):
+    """Lists for the roots and their children (nodes with >= 9 empties here)
+    replace the fastest-first order: scores stay exact, node counts change."""
     p, o, scores = c1
-    lists = np.zeros(len(p), np.uint64)
-    used = 0
+
+    def moves_of(a, b):
+        legal = oracle.L.orc_mobility(a, b)
+        return [k for k in range(64) if (legal >> k) & 1]
+
+    entries = {}
     for i in range(len(p)):
-        legal = oracle.L.orc_mobility(int(p[i]), int(o[i]))
-        moves = [k for k in range(64) if (legal >> k) & 1]
-        if order == "high_first":
-            moves = moves[::-1]
-        else:  # the move the oracle finds best first
-            _, _, _, b = oracle.solve_batch(p[i:i + 1], o[i:i + 1], mode=1)
-            if 0 <= int(b[0]) < 64:
-                moves.remove(int(b[0]))
-                moves.insert(0, int(b[0]))
-        lists[i] = pack_root_list(moves, len(moves))
-        used += 1
-    sc, bm, _, st = emu(p, o, 10, shared_frames=1, root_lists=lists.ctypes.data, learned_min=10)
-    assert used == len(p)
+        a, b = int(p[i]), int(o[i])
+        nodes = [(a, b)]
+        for k in moves_of(a, b):
+            f = oracle.L.orc_flip(a, b, k)
+            nodes.append((b ^ f, a ^ f ^ (1 << k)))
+        for (x, y) in nodes:
+            ms = moves_of(x, y)
+            if order == "high_first":
+                ms = ms[::-1]
+            else:  # the move the oracle finds best first
+                _, _, _, bst = oracle.solve_batch(np.array([x], np.uint64), np.array([y], np.uint64),
+                                                  mode=1)
+                if 0 <= int(bst[0]) < 64:
+                    ms.remove(int(bst[0]))
+                    ms.insert(0, int(bst[0]))
+            entries[(x, y)] = pack_list(ms, len(ms))
+    table = order_table(entries, 12)
+    _, _, plain_nodes, _ = emu(p, o, 10, shared_frames=1)
+    sc, bm, nodes, st = emu(p, o, 10, shared_frames=1, order_table=table.ctypes.data,
+                            order_bits=12, learned_min=9)
     assert np.array_equal(sc.astype(int), scores) and st[6] == 0
+    assert not np.array_equal(nodes, plain_nodes)
