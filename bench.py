@@ -26,9 +26,10 @@ the timed region.
 The transposition table is always on; the line reports its size, probes,
 hits, updates and 32-byte-sector traffic rate.  A stratified sample of the
 scores is checked against the oracle outside the timed region
-(`parity_sample`).  Options: `--learned` orders the top of the search with
-the learned move orderer (weights trained by the library's own GPU kernels,
-loaded from a file); `--tuned` autotunes the launch and search parameters on
+(`parity_sample`).  The top of the search (nodes with >= 14 empties in the
+first two plies) is ordered by the learned move orderer, whose weights were
+trained by the library's own GPU kernels and are loaded from a file
+(`--no-learned`: fastest-first only).  Options: `--tuned` autotunes the launch and search parameters on
 a sample of the batch first (untimed); `--plain` also times the plain kernel
 on the same batch; `--table-bits` sets the table size.
 
@@ -239,9 +240,9 @@ def main():
     ap.add_argument("--table-bits", type=int, default=0,
                     help="transposition table of 2^bits entries (0 = library default: 2^28 on "
                          "a device with >= 64 GiB)")
-    ap.add_argument("--learned", action="store_true",
-                    help="order the top of the search with the learned move orderer "
-                         "(weights from --weights)")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="fastest-first ordering only (by default the top of the search is "
+                         "ordered by the learned move orderer, weights from --weights)")
     ap.add_argument("--weights", default=os.path.join(ROOT, "gpuothello2_gb300", "data",
                                                       "orderer.f32"))
     ap.add_argument("--tuned", action="store_true",
