@@ -18,9 +18,11 @@
 //   - transposition table (table.cuh) at nodes with >= tt_min empties: a
 //     probe when the node is created (a bound outside the window closes it,
 //     one inside narrows the window) and a bound stored when it closes;
-//   - stability cutoff at nodes with >= stab_min empties: discs of the
-//     opponent that can never flip cap the side to move's score at
-//     64 - 2 * stable, which closes a node whose alpha is at or above it;
+//   - stability cutoff at nodes with >= stab_min empties and alpha >=
+//     stab_gate + 3 * empties: discs of the opponent that can never flip cap
+//     the side to move's score at 64 - 2 * stable, which closes a node whose
+//     alpha is at or above it (lopsided positions, the slowest to solve,
+//     gain most);
 //   - a move at a node with two empties scores its child (one empty) in the
 //     same step: the child's last move needs only a flip count;
 //   - passes happen in place with the window negated and swapped
@@ -758,7 +760,9 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
           }
         }
       }
-      if (!closed && args.stab_min && E >= args.stab_min && alpha >= args.stab_gate) {
+      // the cutoff needs about (64 - alpha) / 2 stable discs; few empties leave
+      // many stable discs, so the alpha it is worth checking at rises with E
+      if (!closed && args.stab_min && E >= args.stab_min && alpha >= args.stab_gate + 3 * E) {
         const int cap = 64 - 2 * stable_count(O, P | O);
         if (cap <= alpha) {  // the side to move cannot reach alpha
           best = cap;

@@ -210,8 +210,8 @@ int check_options(const gpo_options* opt) {
 }
 
 // Defaults of the batched search (the autotuner can choose others per GPU):
-// fastest-first from 6 empties, table from 7, the stability cutoff from 6
-// empties when alpha >= 30, helping from 7.
+// fastest-first from 6 empties, table from 7, the stability cutoff from 4
+// empties when alpha >= 10 + 3 * empties, helping from 7.
 constexpr int kDefaultFF = 6;
 constexpr int kDefaultTableMin = 7;
 // Table size: tens of thousands of searches run at once and share it, so
@@ -222,8 +222,8 @@ constexpr int kDefaultTableBitsSmall = 24;
 int default_table_bits(const Context* c) {
   return c->mem >= (static_cast<size_t>(64) << 30) ? kDefaultTableBitsLarge : kDefaultTableBitsSmall;
 }
-constexpr int kDefaultStabMin = 6;
-constexpr int kDefaultStabGate = 30;
+constexpr int kDefaultStabMin = 4;
+constexpr int kDefaultStabGate = 10;
 constexpr int kDefaultHelpMin = 7;
 
 // Bucketing, learned root orders and the persistent search, enqueued on s;

@@ -27,7 +27,7 @@ struct BatchedArgs {
   DeviceStats* stats;
   int ff;                // fastest-first ordering at nodes with >= ff empties
   int stab_min;          // stability cutoff at nodes with >= stab_min empties (0 = off) ...
-  int stab_gate;         // ... whose alpha is at least stab_gate
+  int stab_gate;         // ... whose alpha is at least stab_gate + 3 * empties
   int help_min;          // split nodes need >= help_min empties (0 = no helping)
   int roots_per_warp;    // input positions a warp searches at once (1..32)
   // Frame slots: a node with E empties saves its frame in slot E (3..depth)

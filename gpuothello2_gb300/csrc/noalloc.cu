@@ -120,8 +120,8 @@ extern "C" int solve_batch_device_noalloc(const uint64_t* d_player, const uint64
   a.score = reinterpret_cast<signed char*>(d_score);
   a.stats = stats;
   a.ff = 6;
-  a.stab_min = 6;
-  a.stab_gate = 30;
+  a.stab_min = 4;
+  a.stab_gate = 10;
   a.help_min = 7;
   a.wait_limit_ns = 600000ULL * 1000000ULL;
   BatchedLaunch cfg;

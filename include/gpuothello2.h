@@ -76,8 +76,8 @@ typedef struct gpo_options {
                                  0 = when they all fit at the register-limited occupancy,
                                  > 0 = only if at most this many are needed, negative = never
                                  (every frame in the global frame array) */
-  int stability_min_empties;  /* stability cutoff at nodes with >= this many empties;
-                                 0 = default (6), negative = off */
+  int stability_min_empties;  /* stability cutoff at nodes with >= this many empties (and
+                                 alpha >= 10 + 3 * empties); 0 = default (4), negative = off */
   int roots_per_warp;         /* input positions a warp searches at once, the rest of its
                                  lanes helping (1..32); 0 = from the batch size: 32 when the
                                  batch fills the GPU, fewer for small batches */
