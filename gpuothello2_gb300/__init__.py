@@ -52,6 +52,7 @@ class Options(ctypes.Structure):
         ("smem_frames", ctypes.c_int),
         ("stability_min_empties", ctypes.c_int),
         ("roots_per_warp", ctypes.c_int),
+        ("hard_nodes", ctypes.c_int64),
         ("root_split_plies", ctypes.c_int),
     ]
 

@@ -334,11 +334,16 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
     if (busy && helper && !abort && ld_shared_volatile(&sp.cut[wbase + towner])) abort = true;
 
     // ---- free lanes take input positions (at most rpw searches of its own
-    //      per warp; the rest of the warp helps) ----
+    //      per warp; the rest of the warp helps).  A warp holding a search
+    //      that has run past hard_nodes takes no new positions: its lanes
+    //      help that search as they come free (the other warps keep taking
+    //      the queue), so the slowest positions get helpers early instead
+    //      of finishing alone after the queue has run out. ----
     const unsigned own = __ballot_sync(kFull, busy && !helper);
+    const bool hard = args.hard_nodes && __any_sync(kFull, busy && !helper && nodes > args.hard_nodes);
     if (!qdone) {
       const unsigned freem = __ballot_sync(kFull, !busy);
-      const int quota = rpw - __popc(own);
+      const int quota = hard ? 0 : rpw - __popc(own);
       if (freem && quota > 0) {
         unsigned takers = freem;
         while (__popc(takers) > quota) takers &= ~(1u << (31 - __clz(static_cast<int>(takers))));
@@ -553,7 +558,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
     // ---- idle lanes take moves of split nodes of their warp ----
     u64 hX = 0, hY = 0;
     const unsigned freem = __ballot_sync(kFull, !busy);
-    const bool can_help = args.help_min > 0 && (qdone || __popc(own) >= rpw);
+    const bool can_help = args.help_min > 0 && (qdone || hard || __popc(own) >= rpw);
     if (freem && can_help) {
       // a busy lane without a split node looks for one now and then
       if (busy && !stall && spe == 0 && !abort && (chk & 7u) == 0u && root_e >= args.help_min)

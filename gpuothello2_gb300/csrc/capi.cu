@@ -225,6 +225,7 @@ int default_table_bits(const Context* c) {
 constexpr int kDefaultStabMin = 4;
 constexpr int kDefaultStabGate = 10;
 constexpr int kDefaultHelpMin = 7;
+constexpr unsigned long long kDefaultHardNodes = 1ULL << 23;
 
 // Bucketing, learned root orders and the persistent search, enqueued on s;
 // waits for them and returns the status.
@@ -277,6 +278,8 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   a.help_min = o.help_min_empties > 0 ? o.help_min_empties
                                       : (o.help_min_empties < 0 ? 0 : kDefaultHelpMin);
   a.node_budget = o.node_budget;
+  a.hard_nodes = o.hard_nodes > 0 ? static_cast<unsigned long long>(o.hard_nodes)
+                                  : (o.hard_nodes < 0 ? 0ULL : kDefaultHardNodes);
   a.order_table = frontier > 0 ? c->dOrder : nullptr;
   a.order_bits = c->order_bits;
   a.learned_min = lmin;

@@ -30,6 +30,8 @@ struct BatchedArgs {
   int stab_gate;         // ... whose alpha is at least stab_gate + 3 * empties
   int help_min;          // split nodes need >= help_min empties (0 = no helping)
   int roots_per_warp;    // input positions a warp searches at once (1..32)
+  unsigned long long hard_nodes;  // a warp with a search past this many nodes takes no new
+                                  // positions, its free lanes help (0 = off)
   // Frame slots: a node with E empties saves its frame in slot E (3..depth)
   // when it pushes a child.  depth <= smem_top: every slot in shared memory;
   // else every slot in the global array gframes (per lane, SoA).

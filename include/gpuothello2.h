@@ -81,6 +81,9 @@ typedef struct gpo_options {
   int roots_per_warp;         /* input positions a warp searches at once, the rest of its
                                  lanes helping (1..32); 0 = from the batch size: 32 when the
                                  batch fills the GPU, fewer for small batches */
+  int64_t hard_nodes;         /* a warp whose own search has visited more than this many
+                                 nodes takes no new positions, so its lanes help that search
+                                 as they come free; 0 = default (2^23), negative = off */
   int root_split_plies;       /* batches with fewer positions than 1/8 of the GPU's warps
                                  (depth >= 14): 0 = expanded on the host until the frontier
                                  fills the GPU (at most 3 plies; positions with <= 12 empties
