@@ -56,9 +56,9 @@ W_NODE = 418  # INT32 ops per node: mobility + flip + make-move of the reference
 # of one batched-kernel launch, from one ncu capture of a smaller launch
 # (profiles/batched_kernel_ncu.md), scaled to this launch by its node count:
 # the traffic is the transposition table's, which grows with the nodes.
-TRAFFIC_BYTES_PER_NODE = (4.026357e9 + 2.894098e9) / 3.639e9
-TRAFFIC_SOURCE = ("ncu capture of 131,072 positions x 12 empties (6.92 GB in 3.64e9 nodes), "
-                  "scaled by nodes")
+TRAFFIC_BYTES_PER_NODE = (6.700996e9 + 3.144086e9) / 3303996693
+TRAFFIC_SOURCE = ("ncu capture of 131,072 positions x 12 empties (9.85 GB in 3.30e9 nodes, "
+                  "profiles/batched_kernel_ncu.md), scaled by nodes")
 SEED, N_POS, LO, HI, DEPTH = 2, 1 << 20, 8, 16, 16
 METRIC = "exact-solved positions/s at 8\u201316 empties: batched+learned vs plain, same GB300"
 WORKLOAD = ("1,048,576 positions, random playouts seed 2, empties uniform 8..16, DEPTH 16")
@@ -226,6 +226,57 @@ def parity_sample(p, o, scores, threads=0):
                    "own alpha-beta (orc_solve_fast), outside the timed region"}
 
 
+def profile_cases(args):
+    """Small runs for profiling (ncu) and peak probes; no JSON line.
+    --profile-solve N E: N positions (seed 1) at E empties, solved twice with the
+    library defaults and the learned orderer (capture the second launch:
+    `ncu ... -k regex:batched_kernel -s 1 -c 1 ...`); --profile-think N D: think
+    mode with 13 patterns of 5-12 squares and seeded random weights, N positions
+    (seed 6, 24..34 empties) to D plies, twice; --int-peak: the INT32 issue rates
+    measured by libgpo_intpeak."""
+    import numpy as np
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import gpuothello2_gb300 as g
+    from gpuothello2_gb300 import build as B
+
+    if args.int_peak:
+        lib = ctypes.CDLL(B.INTPEAK_LIB)
+        lib.gpo_int_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]
+        for op, name in ((0, "lop3.b32"), (1, "add.u32")):
+            v, ms = ctypes.c_double(), ctypes.c_double()
+            if lib.gpo_int_peak(op, ctypes.byref(v), ctypes.byref(ms)) != 0:
+                raise RuntimeError("gpo_int_peak failed")
+            print("int peak %s: %.3f Tops/s (%.3f ms per launch)" % (name, v.value / 1e12,
+                                                                     ms.value), flush=True)
+    if args.profile_solve:
+        n, e = args.profile_solve
+        g.mlp_load(np.fromfile(args.weights, dtype=np.float32))
+        p, o = g.generate(1, n, e, e)
+        for _ in range(2):
+            _, _, _, st, _ = g.solve(p, o, e)
+        print("solve n=%d empties=%d nodes=%d kernel_ms=%.1f" % (n, e, st.nodes, st.kernel_ms),
+              flush=True)
+    if args.profile_think:
+        n, depth = args.profile_think
+        # 4 rows, 2 diagonals, corner blocks, an edge with its X squares and
+        # shorter lines: 13 patterns of 5 to 12 squares
+        masks = [0xFF << (8 * r) for r in range(4)] + [
+            0x8040201008040201, 0x0102040810204080, 0x1F1F, 0x070707, 0x42FF, 0x0F0F0F, 0x1F,
+            0x804020100804, 0x3C3C]
+        rng = np.random.default_rng(1)
+        g.eval_load(masks, rng.uniform(-4, 4, sum(3 ** bin(m).count("1") for m in masks)), 0.5)
+        p, o = g.generate(6, n, 24, 34)
+        for _ in range(2):
+            _, _, _, st, _ = g.think(p, o, depth)
+        sec = st.kernel_ms / 1e3
+        print("think n=%d depth=%d kernel_ms=%.3f positions/s=%.4g nodes/s=%.4g" %
+              (n, depth, st.kernel_ms, n / sec, st.nodes / sec), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -248,7 +299,13 @@ def main():
     ap.add_argument("--tuned", action="store_true",
                     help="autotune launch/search parameters on a 4,096-position sample of the "
                          "batch first (untimed; cached per GPU, depth and empties range)")
+    ap.add_argument("--profile-solve", type=int, nargs=2, metavar=("N", "EMPTIES"))
+    ap.add_argument("--profile-think", type=int, nargs=2, metavar=("N", "DEPTH"))
+    ap.add_argument("--int-peak", action="store_true")
     args = ap.parse_args()
+    if args.profile_solve or args.profile_think or args.int_peak:
+        profile_cases(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -475,6 +475,7 @@ __global__ void frontier_kernel(const u64* __restrict__ P, const u64* __restrict
 }
 
 constexpr int kOrderProbe = 16;
+constexpr int kInferRows = 1 << 18;
 
 __global__ void order_insert_kernel(const u64* __restrict__ fP, const u64* __restrict__ fO,
                                     const u64* __restrict__ lists, long off, long count, int rows,
@@ -733,9 +734,11 @@ int gpo_mlp_load(const float* w) {
     return GPO_OK;
   }
   if (!g_loaded) {
-    int rc = net_alloc(g_infer, 1 << 16, false);
+    // rows per inference batch: the learned order table scores millions of
+    // frontier positions per solve, in batches of this many
+    int rc = net_alloc(g_infer, kInferRows, false);
     if (rc != GPO_OK) return rc;
-    if (cudaMalloc(&g_lists_tmp, (1 << 16) * sizeof(u64)) != cudaSuccess) return GPO_ERR_NOMEM;
+    if (cudaMalloc(&g_lists_tmp, kInferRows * sizeof(u64)) != cudaSuccess) return GPO_ERR_NOMEM;
   }
   int rc = upload_weights(g_infer, w, nullptr);
   if (rc != GPO_OK) return rc;
