@@ -241,15 +241,7 @@ __device__ __noinline__ int find_split_node(Frames fr, SplitState sp, int t, u64
 
 }  // namespace
 
-__device__ __forceinline__ unsigned long long global_ns() {
-#ifdef GPO_SIMT_EMU  // the CPU emulation of this kernel used by the tests
-  return gpo_emu_ns();
-#else
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-#endif
-}
+__device__ __forceinline__ unsigned long long global_ns() { return gpo_global_ns(); }
 
 // Blocks per SM the register allocation must allow (128-thread blocks).
 #ifndef GPO_BATCHED_MIN_BLOCKS

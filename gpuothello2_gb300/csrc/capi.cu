@@ -546,7 +546,9 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
   if (o.method == GPO_METHOD_PLAIN) {
     GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
     GPO_CK(cudaEventRecord(c->ev0, s));
-    GPO_CK(launch_plain(dP, dO, n, depth, dScore, dNodes, c->dStats, s));
+    const unsigned long long limit =
+        static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 600000) * 1000000ULL;
+    GPO_CK(launch_plain(dP, dO, n, depth, dScore, dNodes, c->dStats, limit, s));
     c->launches += 1;
     GPO_CK(cudaEventRecord(c->ev1, s));
     DeviceStats hs;

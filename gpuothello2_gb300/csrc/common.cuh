@@ -39,7 +39,19 @@ struct DeviceStats {
   unsigned long long stab_cuts;  // nodes closed by the stability cutoff
   unsigned int status;
   unsigned int next;             // work-queue cursor of the persistent kernel
+  unsigned long long t0;         // plain kernel: global timer at its first block's start
 };
+
+// The GPU's global nanosecond timer (launch deadlines).
+__device__ __forceinline__ unsigned long long gpo_global_ns() {
+#ifdef GPO_SIMT_EMU  // the CPU emulation of the kernels used by the tests
+  return gpo_emu_ns();
+#else
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+#endif
+}
 
 __device__ __forceinline__ int ctz64(u64 x) { return __ffsll(static_cast<long long>(x)) - 1; }
 

@@ -60,8 +60,11 @@ struct BatchedLaunch {
   size_t smem;      // out: dynamic shared memory per block
 };
 
+// limit_ns: deadline of the launch from its first block's start; positions
+// still running then stop and the call reports GPO_ERR_TIMEOUT.
 cudaError_t launch_plain(const u64* player, const u64* opp, int n, int depth, signed char* score,
-                         unsigned long long* nodes_out, DeviceStats* stats, cudaStream_t s);
+                         unsigned long long* nodes_out, DeviceStats* stats,
+                         unsigned long long limit_ns, cudaStream_t s);
 cudaError_t launch_bucket(const u64* player, const u64* opp, int n, int depth, unsigned* hist,
                           unsigned* cursor, unsigned* perm, DeviceStats* stats, int sms,
                           cudaStream_t s);

@@ -70,7 +70,7 @@ __device__ __forceinline__ u64 scan_pick(u64 moves) {
 __global__ void __launch_bounds__(kPlainBlock)
 plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n, int depth,
              signed char* __restrict__ score, unsigned long long* __restrict__ nodes_out,
-             DeviceStats* __restrict__ stats) {
+             DeviceStats* __restrict__ stats, unsigned long long limit_ns) {
   __shared__ u64 sP[kPlainLower][kPlainBlock];
   __shared__ u64 sO[kPlainLower][kPlainBlock];
   __shared__ u64 sM[kPlainLower][kPlainBlock];
@@ -78,7 +78,10 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
   __shared__ __align__(16) u64 rays[256];
   PlainUpper up[kMaxEmpties - 8];
   gpo_build_rays(rays);
+  // One deadline for the launch: the first block to start stamps the time.
+  if (threadIdx.x == 0) atomicCAS(&stats->t0, 0ULL, gpo_global_ns());
   __syncthreads();
+  const unsigned long long deadline = *reinterpret_cast<volatile unsigned long long*>(&stats->t0) + limit_ns;
 
   const int t = threadIdx.x;
   const int i = blockIdx.x * blockDim.x + t;
@@ -98,6 +101,10 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
       cnt = plain_upper_moves(P, O, up[0].list, rays);
       nodes = 1;
       for (;;) {
+        if ((nodes & 4095) == 0 && gpo_global_ns() > deadline) {  // past the launch deadline
+          atomicOr(&stats->status, kErrWait);
+          break;
+        }
         // Each pass either pushes a child / passes in place (continue) or
         // falls through to the commit at the bottom.
         if (level < U) {
@@ -228,9 +235,11 @@ plain_kernel(const u64* __restrict__ player, const u64* __restrict__ opp, int n,
 }
 
 cudaError_t launch_plain(const u64* player, const u64* opp, int n, int depth, signed char* score,
-                         unsigned long long* nodes_out, DeviceStats* stats, cudaStream_t s) {
+                         unsigned long long* nodes_out, DeviceStats* stats,
+                         unsigned long long limit_ns, cudaStream_t s) {
   const int grid = (n + kPlainBlock - 1) / kPlainBlock;
-  plain_kernel<<<grid, kPlainBlock, 0, s>>>(player, opp, n, depth, score, nodes_out, stats);
+  plain_kernel<<<grid, kPlainBlock, 0, s>>>(player, opp, n, depth, score, nodes_out, stats,
+                                            limit_ns);
   return cudaGetLastError();
 }
 

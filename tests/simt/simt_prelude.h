@@ -146,6 +146,11 @@ inline unsigned atomicCAS(unsigned* p, unsigned cmp, unsigned v) {
   __atomic_compare_exchange_n(p, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
   return cmp;
 }
+inline unsigned long long atomicCAS(unsigned long long* p, unsigned long long cmp,
+                                    unsigned long long v) {
+  __atomic_compare_exchange_n(p, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+  return cmp;
+}
 inline unsigned atomicMax(unsigned* p, unsigned v) {
   unsigned old = __atomic_load_n(p, __ATOMIC_SEQ_CST);
   while (old < v &&
