@@ -33,6 +33,7 @@ EXPORTED_SYMBOLS = (
     "gpo_device_info", "solve_batch_device_noalloc", "gpo_mlp_param_count", "gpo_mlp_init",
     "gpo_mlp_forward", "gpo_mlp_gradients", "gpo_mlp_train", "gpo_mlp_load",
     "gpo_eval_load", "gpo_eval_load_files", "gpo_evaluate", "think_batch",
+    "gpo_graph_create", "gpo_graph_launch", "gpo_graph_stats", "gpo_graph_destroy",
 )
 
 
@@ -120,6 +121,12 @@ def lib():
         L.gpo_eval_load_files.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
         L.gpo_evaluate.argtypes = [vp, vp, i, vp]
         L.think_batch.argtypes = [vp, vp, i, i, vp, vp, vp, ctypes.POINTER(Stats)]
+        L.gpo_graph_create.argtypes = [vp, vp, i, i, vp, ctypes.POINTER(Options),
+                                       ctypes.POINTER(vp)]
+        L.gpo_graph_launch.argtypes = [vp, vp]
+        L.gpo_graph_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.gpo_graph_destroy.argtypes = [vp]
+        L.gpo_graph_destroy.restype = None
         _lib = L
     return _lib
 

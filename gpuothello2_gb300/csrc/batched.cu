@@ -840,6 +840,12 @@ size_t batched_gframe_bytes(int depth, int smem_top, size_t lanes) {
   return static_cast<size_t>(depth > 2 ? depth - 2 : 0) * kFrameBytes * lanes;
 }
 
+cudaError_t launch_batched_shape(const BatchedArgs& args, int grid, int threads, size_t smem,
+                                 cudaStream_t s) {
+  batched_kernel<<<grid, threads, smem, s>>>(args);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_batched(const BatchedArgs& args, BatchedLaunch& cfg, int sms, cudaStream_t s) {
   const int threads = cfg.threads > 0 ? cfg.threads : 128;
   int grid = 0;

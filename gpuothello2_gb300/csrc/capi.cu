@@ -578,6 +578,121 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
   return run_batched(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats);
 }
 
+// ---- CUDA graphs of a batched solve (repeated batches) ----
+// The batched path without the learned ordering or the root split is a
+// fixed sequence of stream work: clear the counters, bucket, clear the
+// table, search, copy the counters out.  For a caller that solves batch
+// after batch in the same device arrays, that sequence is captured once into
+// a CUDA graph and replayed: one graph launch instead of seven API calls
+// and launches, and no host work between them.  The graph owns every buffer
+// it touches, so solves through the other entry points (which may grow the
+// context's buffers) never move memory under it.
+struct GraphState {
+  int device = -1;
+  int n = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;
+  unsigned* perm = nullptr;
+  unsigned* hist = nullptr;
+  unsigned* cursor = nullptr;
+  DeviceStats* stats = nullptr;
+  DeviceStats* host_stats = nullptr;  // pinned: the replay's counters
+  unsigned char* frames = nullptr;
+  unsigned long long* table = nullptr;
+  int table_bits = 0;
+  int launches = 0;
+};
+
+void graph_free(GraphState* g) {
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->capture) cudaStreamDestroy(g->capture);
+  cudaFree(g->perm);
+  cudaFree(g->hist);
+  cudaFree(g->cursor);
+  cudaFree(g->stats);
+  cudaFree(g->frames);
+  cudaFree(g->table);
+  cudaFreeHost(g->host_stats);
+  delete g;
+}
+
+int graph_build(GraphState* g, const Context* c, const u64* dP, const u64* dO, int n, int depth,
+                signed char* dScore, const gpo_options& o) {
+  g->device = c->device;
+  g->n = n;
+  GPO_CK(cudaMalloc(&g->perm, static_cast<size_t>(n) * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&g->hist, 65 * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&g->cursor, 65 * sizeof(unsigned)));
+  GPO_CK(cudaMalloc(&g->stats, sizeof(DeviceStats)));
+  GPO_CK(cudaMallocHost(&g->host_stats, sizeof(DeviceStats)));
+  std::memset(g->host_stats, 0, sizeof(DeviceStats));
+  BatchedArgs a = {};
+  a.player = dP;
+  a.opp = dO;
+  a.perm = g->perm;
+  a.n = n;
+  a.depth = depth;
+  a.score = dScore;
+  a.stats = g->stats;
+  a.ff = o.fastest_first_empties > 0 ? o.fastest_first_empties : kDefaultFF;
+  a.stab_min = o.stability_min_empties > 0 ? o.stability_min_empties
+                                           : (o.stability_min_empties < 0 ? 0 : kDefaultStabMin);
+  a.stab_gate = kDefaultStabGate;
+  a.help_min = o.help_min_empties > 0 ? o.help_min_empties
+                                      : (o.help_min_empties < 0 ? 0 : kDefaultHelpMin);
+  a.node_budget = o.node_budget;
+  a.hard_nodes = o.hard_nodes > 0 ? static_cast<unsigned long long>(o.hard_nodes)
+                                  : (o.hard_nodes < 0 ? 0ULL : kDefaultHardNodes);
+  a.learned_min = 64;
+  a.wait_limit_ns =
+      static_cast<unsigned long long>(o.wait_limit_ms > 0 ? o.wait_limit_ms : 600000) * 1000000ULL;
+  const int threads = o.threads_per_block > 0 ? o.threads_per_block : 128;
+  GPO_CK(batched_plan(threads, depth, &a.smem_top));
+  if (o.smem_frames < 0 || (o.smem_frames > 0 && o.smem_frames < depth - 2)) a.smem_top = 2;
+  int grid = 0;
+  size_t smem = 0;
+  GPO_CK(batched_grid(threads, a.smem_top, c->sms, &grid, &smem));
+  const long warps = static_cast<long>(grid) * (threads / 32);
+  if (o.roots_per_warp > 0) {
+    a.roots_per_warp = o.roots_per_warp;
+  } else {
+    const long per = (n + warps - 1) / warps;
+    a.roots_per_warp = static_cast<int>(per < 1 ? 1 : (per > 32 ? 32 : per));
+  }
+  const size_t fbytes = batched_gframe_bytes(depth, a.smem_top, static_cast<size_t>(grid) * threads);
+  if (fbytes) GPO_CK(cudaMalloc(&g->frames, fbytes));
+  a.gframes = g->frames;
+  if (o.use_table != 0) {
+    g->table_bits = o.table_bits > 0 ? o.table_bits : default_table_bits(c);
+    GPO_CK(cudaMalloc(&g->table, static_cast<size_t>(16) << g->table_bits));
+    a.tt = g->table;
+    a.tt_bits = g->table_bits;
+    a.tt_min = o.table_min_empties > 0 ? o.table_min_empties : kDefaultTableMin;
+  }
+  GPO_CK(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking));
+  cudaStream_t s = g->capture;
+  GPO_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaMemsetAsync(g->stats, 0, sizeof(DeviceStats), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->hist, 0, 65 * sizeof(unsigned), s);
+  if (e == cudaSuccess) e = launch_bucket(dP, dO, n, depth, g->hist, g->cursor, g->perm, g->stats,
+                                          c->sms, s);
+  if (e == cudaSuccess && g->table)
+    e = cudaMemsetAsync(g->table, 0, static_cast<size_t>(16) << g->table_bits, s);
+  if (e == cudaSuccess) e = launch_batched_shape(a, grid, threads, smem, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g->host_stats, g->stats, sizeof(DeviceStats), cudaMemcpyDeviceToHost, s);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+  g->graph = graph;
+  if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  GPO_CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
+  g->launches = 4;  // bucketing (3) and the search
+  return GPO_OK;
+}
+
 int validate_call(const void* a, const void* b, const void* out, int n, int depth) {
   if (n < 0) return GPO_ERR_ARG;
   if (n > 0 && (!a || !b || !out)) return GPO_ERR_ARG;
@@ -710,6 +825,65 @@ void solve_shutdown(void) {
     g_ctx[d] = nullptr;
   }
   if (cur >= 0) cudaSetDevice(cur);
+}
+
+int gpo_graph_create(const uint64_t* d_player, const uint64_t* d_opp, int n, int depth,
+                     int8_t* d_score, const gpo_options* opt, gpo_graph** out) {
+  if (!out) return GPO_ERR_ARG;
+  *out = nullptr;
+  int rc = validate_call(d_player, d_opp, d_score, n, depth);
+  if (rc == GPO_OK) rc = check_options(opt);
+  if (rc != GPO_OK) return rc;
+  if (n == 0) return GPO_ERR_ARG;
+  gpo_options o;
+  gpo_default_options(&o);
+  if (opt) o = *opt;
+  if (o.method != GPO_METHOD_BATCHED || o.use_learned > 0) return GPO_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Context* c = nullptr;
+  if ((rc = ensure_context(&c)) != GPO_OK) return rc;
+  GraphState* g = new GraphState();
+  rc = graph_build(g, c, reinterpret_cast<const u64*>(d_player), reinterpret_cast<const u64*>(d_opp),
+                   n, depth, reinterpret_cast<signed char*>(d_score), o);
+  if (rc != GPO_OK) {
+    graph_free(g);
+    return rc;
+  }
+  *out = reinterpret_cast<gpo_graph*>(g);
+  return GPO_OK;
+}
+
+int gpo_graph_launch(gpo_graph* graph, void* stream) {
+  if (!graph) return GPO_ERR_ARG;
+  GraphState* g = reinterpret_cast<GraphState*>(graph);
+  int dev = -1;
+  GPO_CK(cudaGetDevice(&dev));
+  if (dev != g->device) return GPO_ERR_ARG;
+  GPO_CK(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
+  return GPO_OK;
+}
+
+int gpo_graph_stats(gpo_graph* graph, gpo_stats* stats) {
+  if (!graph || !stats) return GPO_ERR_ARG;
+  const GraphState* g = reinterpret_cast<const GraphState*>(graph);
+  const DeviceStats& hs = *g->host_stats;
+  std::memset(stats, 0, sizeof(*stats));
+  stats->nodes = hs.nodes;
+  stats->table_probes = hs.tt_probes;
+  stats->table_hits = hs.tt_hits;
+  stats->table_updates = hs.tt_updates;
+  stats->splits = hs.handouts;
+  stats->stability_cuts = hs.stab_cuts;
+  stats->table_bits = static_cast<uint64_t>(g->table_bits);
+  stats->launches = static_cast<uint64_t>(g->launches);
+  return status_to_error(hs.status);
+}
+
+void gpo_graph_destroy(gpo_graph* graph) {
+  if (!graph) return;
+  GraphState* g = reinterpret_cast<GraphState*>(graph);
+  cudaStreamSynchronize(g->capture);
+  graph_free(g);
 }
 
 const char* gpo_strerror(int status) {

@@ -69,6 +69,10 @@ cudaError_t launch_bucket(const u64* player, const u64* opp, int n, int depth, u
                           unsigned* cursor, unsigned* perm, DeviceStats* stats, int sms,
                           cudaStream_t s);
 cudaError_t launch_batched(const BatchedArgs& args, BatchedLaunch& cfg, int sms, cudaStream_t s);
+// The launch alone, with a shape from batched_grid (no attribute calls: usable
+// inside a stream capture).
+cudaError_t launch_batched_shape(const BatchedArgs& args, int grid, int threads, size_t smem,
+                                 cudaStream_t s);
 cudaError_t launch_generate(u64 seed, u64 first, int n, int min_e, int max_e, u64* out_p,
                             u64* out_o, cudaStream_t s);
 

@@ -156,6 +156,29 @@ int gpo_generate_device(uint64_t seed, uint64_t first, int n, int min_empties, i
                         uint64_t* d_player, uint64_t* d_opp, void* stream);
 
 /*
+ * Repeated batches as a CUDA graph.  The reference launches one BatchedTask
+ * per batch on its own stream and polls it (main.cu:146-155,
+ * solver.cu:330-333); a caller that solves batch after batch of the same
+ * size in the same device arrays can instead capture the batched solve once
+ * and replay it.  gpo_graph_create captures the solve of n positions held in
+ * d_player/d_opp (scores to d_score) with the given options (NULL =
+ * defaults; the learned ordering and the root split of small batches need
+ * host decisions and are left out: use_learned must not be 1); the graph owns
+ * its scratch and table.  gpo_graph_launch replays it on `stream` (NULL =
+ * the legacy default stream) and returns at once: refill the inputs in place
+ * between replays, ordered on the same stream.  gpo_graph_stats, after the
+ * stream has finished, gives the last replay's counters and status
+ * (GPO_ERR_* for rejected inputs or an exceeded deadline).  A graph is bound
+ * to the device current at its creation.
+ */
+typedef struct gpo_graph gpo_graph;
+int gpo_graph_create(const uint64_t* d_player, const uint64_t* d_opp, int n, int depth,
+                     int8_t* d_score, const gpo_options* opt, gpo_graph** graph);
+int gpo_graph_launch(gpo_graph* graph, void* stream);
+int gpo_graph_stats(gpo_graph* graph, gpo_stats* stats);
+void gpo_graph_destroy(gpo_graph* graph);
+
+/*
  * No counterpart in the reference.  The batched solver for callers that
  * cannot allocate device memory (a host program whose pool allocator owns
  * all device memory, a plugin that may not allocate after start-up, code that

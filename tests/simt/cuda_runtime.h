@@ -138,3 +138,33 @@ inline cudaError_t cudaOccupancyMaxActiveBlocksPerMultiprocessor(int* n, F, int,
 inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 inline const char* cudaGetErrorName(cudaError_t) { return "simtError"; }
 inline const char* cudaGetErrorString(cudaError_t) { return "error in the SIMT emulation"; }
+
+// ---- CUDA graphs: not emulated (capture reports "not supported") ----
+struct SimtGraph {
+  int unused;
+};
+typedef SimtGraph* cudaGraph_t;
+typedef SimtGraph* cudaGraphExec_t;
+enum cudaStreamCaptureMode { cudaStreamCaptureModeThreadLocal = 1 };
+static const cudaError_t cudaErrorNotSupported = 801;
+inline cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) {
+  return cudaErrorNotSupported;
+}
+inline cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t* g) {
+  *g = nullptr;
+  return cudaErrorNotSupported;
+}
+inline cudaError_t cudaGraphInstantiate(cudaGraphExec_t*, cudaGraph_t, unsigned long long) {
+  return cudaErrorNotSupported;
+}
+inline cudaError_t cudaGraphLaunch(cudaGraphExec_t, cudaStream_t) { return cudaErrorNotSupported; }
+inline cudaError_t cudaGraphDestroy(cudaGraph_t) { return cudaSuccess; }
+inline cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
+inline cudaError_t cudaMallocHost(void* p, size_t n) {
+  *static_cast<void**>(p) = std::malloc(n ? n : 1);
+  return cudaSuccess;
+}
+inline cudaError_t cudaFreeHost(void* p) {
+  std::free(p);
+  return cudaSuccess;
+}
