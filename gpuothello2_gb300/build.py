@@ -3,6 +3,7 @@
   lib/libgpuothello2.so  CUDA kernels + C ABI (include/gpuothello2.h), sm_103a
   bin/solver             C++ CLI `solver INPUT OUTPUT DEPTH` over the C ABI
   bin/gen_boards         C++ board-file generator over the C ABI
+  bin/diff_results       C++ result-file differ keyed by board (host only)
   oracle/lib/liboracle.so  CPU oracle (test infrastructure, not the product)
   oracle/lib/libthink_host.so, libbatched_emu.so  csrc/think.cuh and batched.cu
                          compiled for the CPU (built on demand by the tests)
@@ -31,6 +32,7 @@ OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB = os.path.join(LIB_DIR, "libgpuothello2.so")
 SOLVER_BIN = os.path.join(BIN_DIR, "solver")
 GEN_BIN = os.path.join(BIN_DIR, "gen_boards")
+DIFF_BIN = os.path.join(BIN_DIR, "diff_results")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "lib", "liboracle.so")
 # test infrastructure, built on demand by the CPU tests: csrc/think.cuh
@@ -106,6 +108,10 @@ def build_host():
         src = os.path.join(HOST, main)
         if _stale(out, [src] + deps):
             jobs.append([cxx] + flags + [src] + common + ["-o", out] + link)
+    # the result differ is host code only (no GPU library)
+    src = os.path.join(HOST, "diff_main.cpp")
+    if _stale(DIFF_BIN, [src] + common + _headers(HOST)):
+        jobs.append([cxx] + flags + [src] + common + ["-o", DIFF_BIN])
     if jobs:
         with ThreadPoolExecutor(len(jobs)) as ex:
             list(ex.map(_run, jobs))

@@ -12,8 +12,17 @@
 // empties than DEPTH, a missing evaluator file, CUDA failures) end with a
 // message and a nonzero exit instead of undefined behaviour.
 //
-// Environment: GPO_METHOD=plain selects the plain thread-per-board kernel
-// for solve mode (default: batched).
+// Environment (solve mode):
+//   GPO_METHOD=plain      the plain thread-per-board kernel (default: batched)
+//   GPO_TABLE=0           no transposition table (default: on; the stderr line
+//                         "table update count / hit / find" reports its counters,
+//                         the reference's Table counters, main.cu:158-162)
+//   GPO_TABLE_BITS=n      a table of 2^n entries (default: from the device memory)
+//   GPO_WEIGHTS=FILE      learned move-orderer weights (gpo_mlp_load); default: the
+//                         weights shipped beside the binary (../data/orderer.f32),
+//                         used when present; GPO_WEIGHTS=none turns the orderer off
+#include <unistd.h>
+
 #include <chrono>
 #include <cinttypes>
 #include <cstdio>
@@ -31,6 +40,28 @@ long parse_int(const char* s) {
   char* end = nullptr;
   const long v = std::strtol(s, &end, 10);
   return (end && *end == '\0' && end != s) ? v : -1;
+}
+
+// Directory of the running binary (Linux), with a trailing slash; "" if unknown.
+std::string exe_dir() {
+  char buf[4096];
+  const ssize_t k = readlink("/proc/self/exe", buf, sizeof(buf) - 1);
+  if (k <= 0) return "";
+  buf[k] = '\0';
+  std::string s(buf);
+  const size_t slash = s.rfind('/');
+  return slash == std::string::npos ? "" : s.substr(0, slash + 1);
+}
+
+// Loads move-orderer weights from `path` (gpo_mlp_param_count() floats);
+// false if the file is missing or short.
+bool load_weights(const std::string& path) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  std::vector<float> w(static_cast<size_t>(gpo_mlp_param_count()));
+  const size_t got = std::fread(w.data(), sizeof(float), w.size(), f);
+  std::fclose(f);
+  return got == w.size() && gpo_mlp_load(w.data()) == GPO_OK;
 }
 
 int think_main(char** argv) {
@@ -119,6 +150,21 @@ int main(int argc, char** argv) {
   gpo_default_options(&opt);
   const char* method = std::getenv("GPO_METHOD");
   if (method && std::strcmp(method, "plain") == 0) opt.method = GPO_METHOD_PLAIN;
+  const char* table = std::getenv("GPO_TABLE");
+  if (table && std::strcmp(table, "0") == 0) opt.use_table = 0;
+  const char* bits = std::getenv("GPO_TABLE_BITS");
+  if (bits) opt.table_bits = static_cast<int>(parse_int(bits));
+  const char* weights = std::getenv("GPO_WEIGHTS");
+  opt.use_learned = 0;
+  if (opt.method == GPO_METHOD_BATCHED && !(weights && std::strcmp(weights, "none") == 0)) {
+    const std::string wpath = weights ? std::string(weights) : exe_dir() + "../data/orderer.f32";
+    if (load_weights(wpath)) {
+      opt.use_learned = 1;
+    } else if (weights) {
+      std::fprintf(stderr, "cannot load move-orderer weights from %s\n", wpath.c_str());
+      return EXIT_FAILURE;
+    }
+  }
   gpo_stats st;
   std::memset(&st, 0, sizeof(st));
   std::fprintf(stderr, "start!\n");

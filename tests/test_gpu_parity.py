@@ -1,6 +1,7 @@
 """GPU parity: both CUDA methods against the reference's golden scores and
 the CPU oracle, through the C ABI.  Bit-exact everywhere (integer scores)."""
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -238,3 +239,42 @@ def test_table_options_are_checked(gpu):
     assert rc == gpu.GPO_ERR_ARG
     sc, _, _, st, _ = gpu.solve(p, o, 10, use_table=0)
     assert np.array_equal(sc.astype(int), scores) and st.table_probes == 0
+
+
+def test_gen_boards_writes_the_golden_board_file(gpu, tmp_path):
+    """`gen_boards OUT N SEED MIN [MAX]` writes the stream the golden board
+    file holds, byte for byte."""
+    from gpuothello2_gb300 import build
+
+    out = tmp_path / "c1.txt"
+    r = subprocess.run([build.GEN_BIN, str(out), "4096", "0", "10"], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert out.read_text() == open(os.path.join(GOLDEN, "c1_seed0_e10.txt")).read()
+
+
+def test_cli_table_counters_and_switches(gpu, tmp_path):
+    """The CLI's reference-format stderr line carries the table's counters
+    (update count, hit, find) with the table on, zeros with GPO_TABLE=0; the
+    learned orderer's weights load by default; the scores stay the
+    reference's throughout."""
+    from gpuothello2_gb300 import build
+
+    src = os.path.join(GOLDEN, "c3_seed2_mixed.txt")
+    ref = [ln.split()[:2] for ln in open(os.path.join(GOLDEN, "c3_seed2_mixed.ref"))]
+    pat = re.compile(r"table update count: (\d+), table hit: (\d+), table find: (\d+)")
+    for env, on in (({}, True), ({"GPO_TABLE": "0"}, False), ({"GPO_WEIGHTS": "none"}, True),
+                    ({"GPO_TABLE_BITS": "20"}, True)):
+        out = tmp_path / "out.txt"
+        r = subprocess.run([build.SOLVER_BIN, src, str(out), "16"], capture_output=True,
+                           text=True, timeout=300, env=dict(os.environ, **env))
+        assert r.returncode == 0, r.stderr
+        upd, hit, find = map(int, pat.search(r.stderr).groups())
+        if on:
+            assert upd > 0 and find > 0 and 0 < hit <= find, r.stderr
+        else:
+            assert upd == hit == find == 0
+        assert [ln.split() for ln in open(out)] == ref
+    r = subprocess.run([build.SOLVER_BIN, src, str(tmp_path / "x"), "16"], capture_output=True,
+                       text=True, timeout=300, env=dict(os.environ, GPO_WEIGHTS="/nonexistent"))
+    assert r.returncode != 0 and "weights" in r.stderr

@@ -128,3 +128,35 @@ def test_ctypes_mirrors_match_the_header_layout(tmp_path):
         assert c_layout[(cname, "size")] == ctypes.sizeof(py), cname
         for field, _ in py._fields_:
             assert c_layout[(cname, field)] == getattr(py, field).offset, (cname, field)
+
+
+def test_result_differ_matches_by_board(built, tmp_path):
+    """diff_results compares result files by board: order and duplicates do
+    not matter; a changed score, a missing board and a board listed with two
+    scores are reported."""
+    import random
+    import subprocess
+
+    ref = [ln.split()[:2] for ln in open(os.path.join(GOLDEN, "c1_seed0_e10.ref"))][:300]
+    a = tmp_path / "a.txt"
+    a.write_text("".join("%s %s\n" % (b, v) for b, v in ref))
+    lines = ref + ref[:17]  # duplicates
+    random.Random(5).shuffle(lines)
+    b = tmp_path / "b.txt"
+    b.write_text("".join("%s %s\n" % (x, v) for x, v in lines))
+    run = lambda x, y: subprocess.run([built.DIFF_BIN, str(x), str(y)], capture_output=True,
+                                      text=True)
+    r = run(a, b)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 differ, 0 only in A, 0 only in B" in r.stdout
+    changed = [list(x) for x in ref]
+    changed[10][1] = str(int(changed[10][1]) + 2)
+    c = tmp_path / "c.txt"
+    c.write_text("".join("%s %s\n" % (x, v) for x, v in changed[1:]))  # board 0 missing
+    r = run(a, c)
+    assert r.returncode == 1
+    assert ("differs: %s %s %s" % (ref[10][0], ref[10][1], changed[10][1])) in r.stdout
+    assert ("only in A: %s %s" % (ref[0][0], ref[0][1])) in r.stdout
+    bad = tmp_path / "bad.txt"
+    bad.write_text("%s %s\n%s %d\n" % (ref[3][0], ref[3][1], ref[3][0], int(ref[3][1]) + 2))
+    assert run(a, bad).returncode == 2
