@@ -499,16 +499,26 @@ __global__ void order_insert_kernel(const u64* __restrict__ fP, const u64* __res
 Net g_infer;        // network loaded for the solver
 u64* g_lists_tmp = nullptr;
 bool g_loaded = false;
-// Guards g_infer / g_loaded: gpo_mlp_load may run on another thread while a
-// solve orders its roots.  (Freeing the network's buffers synchronises the
-// device, so kernels already enqueued finish before the memory goes.)
+int g_infer_device = -1;                 // device holding g_infer
+cudaEvent_t g_infer_done = nullptr;      // recorded after the last inference batch
+// Guards g_infer / g_loaded / g_infer_done.  The mutex is held only while a
+// solve enqueues its inference work on the solve's (non-blocking) stream, so
+// gpo_mlp_load first waits on g_infer_done: a reload never overwrites
+// weights that enqueued inference kernels may still read.
 std::mutex g_mlp_mutex;
+
+bool loaded_here() {
+  int dev = -1;
+  return g_loaded && cudaGetDevice(&dev) == cudaSuccess && dev == g_infer_device;
+}
 
 }  // namespace
 
+// True when a network is loaded on the current device (the network lives on
+// the device that was current at gpo_mlp_load).
 bool mlp_loaded() {
   std::lock_guard<std::mutex> lock(g_mlp_mutex);
-  return g_loaded;
+  return loaded_here();
 }
 
 // Learned order table for the search: the frontier of the `count` roots
@@ -524,7 +534,7 @@ int mlp_order_frontier(const u64* d_player, const u64* d_opp, const unsigned* d_
   *launched = 0;
   *frontier = 0;
   std::lock_guard<std::mutex> lock(g_mlp_mutex);
-  if (!g_loaded) return GPO_ERR_ARG;
+  if (!loaded_here()) return GPO_ERR_ARG;
   Net& t = g_infer;
   MLP_CK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
   MLP_CK(cudaMemsetAsync(table, 0, (static_cast<size_t>(32)) << table_bits, s));
@@ -547,6 +557,7 @@ int mlp_order_frontier(const u64* d_player, const u64* d_opp, const unsigned* d_
                                                               t.rows, table, table_bits);
     MLP_CK(cudaGetLastError());
   }
+  MLP_CK(cudaEventRecord(g_infer_done, s));
   *frontier = total;
   return GPO_OK;
 }
@@ -722,16 +733,28 @@ int gpo_mlp_train(const uint64_t* player, const uint64_t* opp, const int8_t* bes
   return rc;
 }
 
-// Loads weights for the solver's learned root ordering (use_learned);
-// NULL unloads them.
+// Loads weights for the solver's learned ordering (use_learned) on the
+// current device (a load on another device moves the network there); NULL
+// unloads them.
 int gpo_mlp_load(const float* w) {
   std::lock_guard<std::mutex> lock(g_mlp_mutex);
-  if (!w) {
+  // inference that a solve enqueued with the old weights finishes first
+  if (g_infer_done && cudaEventSynchronize(g_infer_done) != cudaSuccess) return GPO_ERR_CUDA;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GPO_ERR_CUDA;
+  if (!w || (g_loaded && dev != g_infer_device)) {
+    // unload, or move the network to the current device
+    if (g_loaded && dev != g_infer_device && cudaSetDevice(g_infer_device) != cudaSuccess)
+      return GPO_ERR_CUDA;
     net_free(g_infer);
     cudaFree(g_lists_tmp);
+    if (g_infer_done) cudaEventDestroy(g_infer_done);
     g_lists_tmp = nullptr;
+    g_infer_done = nullptr;
     g_loaded = false;
-    return GPO_OK;
+    g_infer_device = -1;
+    if (cudaSetDevice(dev) != cudaSuccess) return GPO_ERR_CUDA;
+    if (!w) return GPO_OK;
   }
   if (!g_loaded) {
     // rows per inference batch: the learned order table scores millions of
@@ -739,11 +762,15 @@ int gpo_mlp_load(const float* w) {
     int rc = net_alloc(g_infer, kInferRows, false);
     if (rc != GPO_OK) return rc;
     if (cudaMalloc(&g_lists_tmp, kInferRows * sizeof(u64)) != cudaSuccess) return GPO_ERR_NOMEM;
+    if (!g_infer_done &&
+        cudaEventCreateWithFlags(&g_infer_done, cudaEventDisableTiming) != cudaSuccess)
+      return GPO_ERR_CUDA;
   }
   int rc = upload_weights(g_infer, w, nullptr);
   if (rc != GPO_OK) return rc;
   if (cudaDeviceSynchronize() != cudaSuccess) return GPO_ERR_CUDA;
   g_loaded = true;
+  g_infer_device = dev;
   return GPO_OK;
 }
 

@@ -20,10 +20,12 @@
  *   - `depth` is the reference's DEPTH: the largest number of empty squares
  *     any position of the batch may have (README.md:56-58).  A position with
  *     more empties than `depth` is an error, not undefined behaviour.
- *   - All calls are synchronous and serialised by an internal lock; device
- *     buffers, the stream and the transposition table live in a library
- *     context created on first use on the current CUDA device and released
- *     by solve_shutdown().
+ *   - All calls are synchronous and serialised by an internal lock.  Device
+ *     buffers, the stream and the transposition table live in one library
+ *     context per CUDA device, created on first use on the device current at
+ *     the call (so a caller may switch devices between calls) and released by
+ *     solve_shutdown().  The learned orderer's network lives on the device
+ *     current at gpo_mlp_load; solves on other devices run without it.
  *   - Every entry point returns GPO_OK (0) or a negative GPO_ERR_* status.
  */
 #ifndef GPUOTHELLO2_H
@@ -57,12 +59,13 @@ typedef struct gpo_options {
   int method;                 /* GPO_METHOD_* */
   int use_table;              /* transposition table: 0 off, 1 or -1 (auto) on; cleared at
                                  every call, so no result carries over */
-  int use_learned;            /* learned root ordering (gpo_mlp_load): -1 auto (on when a
-                                 network is loaded), 0 off, 1 on */
+  int use_learned;            /* learned move ordering (gpo_mlp_load): -1 auto (on when a
+                                 network is loaded on this device), 0 off, 1 on */
   int threads_per_block;      /* 32..256, multiple of 32; 0 = 128 */
   int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties;
                                  0 = default (6) */
-  int learned_min_empties;    /* learned ordering at roots with >= this many empties; 0 = 14 */
+  int learned_min_empties;    /* learned ordering at the nodes with >= this many empties in
+                                 the top two plies of each position; 0 = 14 */
   uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog: GPO_ERR_TIMEOUT) */
   int help_min_empties;       /* idle lanes of a warp help its busy lanes with moves of nodes
                                  that have >= this many empties (young brothers wait, after
@@ -188,9 +191,13 @@ void gpo_graph_destroy(gpo_graph* graph);
  * Device input and score arrays as in solve_batch_device; `stream` may be
  * NULL (the legacy default stream).  At most GPO_NOALLOC_MAX_POSITIONS
  * positions (else GPO_ERR_ARG) and depth <= GPO_NOALLOC_MAX_DEPTH (else
- * GPO_ERR_DEPTH).  Splitting and the transposition table are off.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race.
+ * GPO_ERR_DEPTH).  The transposition table and the learned ordering are off;
+ * the lanes of a warp help each other as in solve_batch_device.  When the
+ * frame slots do not fit in shared memory and would not fit the array for the
+ * full grid, the launch uses the largest grid that fits.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * The call returns after its work on `stream` has finished.  Calls share the
+ * array: calls that overlap on the GPU race.
  */
 #define GPO_NOALLOC_MAX_POSITIONS (1 << 20)
 #define GPO_NOALLOC_MAX_DEPTH 16
@@ -203,8 +210,11 @@ int solve_batch_device_noalloc(const uint64_t* d_player, const uint64_t* d_opp, 
  * accumulation, trained on the GPU on best-move labels from
  * solve_batch_ex.  Weights are a flat FP32 array of gpo_mlp_param_count()
  * values: W1[192][256], b1[256], W2[256][256], b2[256], W3[256][64], b3[64].
- * gpo_mlp_load makes the solver order the root moves of positions with
- * >= learned_min_empties empties by the network (scores stay exact).
+ * gpo_mlp_load makes the solver order the moves of the nodes with
+ * >= learned_min_empties empties in the top two plies of each position by
+ * the network (scores stay exact); the nodes are scored in large batches
+ * before the search.  The network is loaded on the current device (NULL
+ * unloads it); a reload waits for inference already enqueued by a solve.
  */
 int gpo_mlp_param_count(void);
 int gpo_mlp_init(uint64_t seed, float* weights);
