@@ -424,7 +424,9 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
             spe = 0;
           }
           // the node closes with value `best`
-          if (!closed && !abort && !passed && args.tt_min && E >= args.tt_min)
+          // (after a pass, P / O / best / beta are those of the position
+          // after the pass, which is the one recorded)
+          if (!closed && !abort && args.tt_min && E >= args.tt_min)
             tt_updates += tt_record(args.tt, args.tt_bits, P, O, best, beta);
           closed = false;
           const int r = passed ? -best : best;
@@ -709,6 +711,10 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
         phase = PH_MASK;
         start_keys = (cm & (cm - 1)) && E >= args.ff;
         if (E == root_e) rootbest = kMovePassDev;
+        // the position after the pass is a node of its own: it gets the table
+        // probe and the stability cutoff (positions where one side keeps
+        // passing are the lopsided ones, whose searches are the longest)
+        created = true;
       }
     } else if (op == OP_MOVE) {
       ++nodes;
