@@ -477,8 +477,10 @@ def main():
                          "(16 B x entries) at the start of every solve also evicts it",
                    "method": ("batched: empties-bucketed persistent queue, per-lane "
                               "principal-variation search with transposition table and "
-                              "stability cutoff, warp-local helping on hard positions; learned "
-                              "ordering %s" % ("on" if args.learned else "off")),
+                              "stability cutoff, warp-local helping on hard positions, the "
+                              "last unfinished positions handed back and finished by a root "
+                              "split over the whole GPU; learned ordering %s"
+                              % ("on" if args.learned else "off")),
                    "table_entries": table_stats["entries"],
                    "tuned": ({"params": tuned, "source": tuned_src} if args.tuned else None),
                    "learned": learned_info},
@@ -495,11 +497,15 @@ def main():
         "nodes_per_s": mean_nodes / mean_kern_s,
         "nodes_per_position": mean_nodes / n,
         "splits_per_step": statistics.mean(st.splits for st in stats),
+        "tail_handoff": {"positions_per_step": statistics.mean(st.tail_positions for st in stats),
+                         "frontier_per_step": statistics.mean(st.root_split_positions
+                                                              for st in stats)},
         "table": table_stats,
         "parity_sample": parity,
         "cpu_baseline": cpu,
         "clocks": sampler.summary(),
-        # counted by the library per call: bucketing (3) and the search (1)
+        # counted by the library per call: bucketing (3) and the search (1),
+        # and the same again for the root split that finishes the tail
         "gpu_launches": launches,
         "plain": plain,
         "speedup_vs_plain": (value / plain["value"]) if plain else None,

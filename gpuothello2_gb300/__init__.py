@@ -55,6 +55,7 @@ class Options(ctypes.Structure):
         ("roots_per_warp", ctypes.c_int),
         ("hard_nodes", ctypes.c_int64),
         ("root_split_plies", ctypes.c_int),
+        ("tail_split_positions", ctypes.c_int),
     ]
 
 
@@ -72,6 +73,7 @@ class Stats(ctypes.Structure):
         ("stability_cuts", ctypes.c_uint64),
         ("table_bits", ctypes.c_uint64),
         ("root_split_positions", ctypes.c_uint64),
+        ("tail_positions", ctypes.c_uint64),
     ]
 
     def as_dict(self):

@@ -156,6 +156,9 @@ __device__ __forceinline__ unsigned ld_shared_volatile(const unsigned* p) {
 __device__ __forceinline__ int ld_shared_volatile(const int* p) {
   return *reinterpret_cast<const volatile int*>(p);
 }
+__device__ __forceinline__ unsigned ld_global_volatile(const unsigned* p) {
+  return *reinterpret_cast<const volatile unsigned*>(p);
+}
 
 // k-th (0-based) set bit of m, m having more than k bits set.
 __device__ __forceinline__ int nth_bit(unsigned m, int k) {
@@ -298,7 +301,8 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
   bool abort = false;   // close every open node at once, reporting nothing
   bool closed = false;  // the current node was closed when created (table or stability)
   bool qdone = false;   // the input queue is used up (warp-uniform)
-  bool late = false;    // the launch deadline has passed (warp-uniform)
+  bool late = false;    // the launch deadline has passed, or the tail is handed back (warp-uniform)
+  bool handoff = false; // the tail is handed back: open positions end unsolved (warp-uniform)
   unsigned pos = 0;     // input position of the search (the owner's for a helper)
   int towner = 0, tsq = 0, tlo = 0, tbeta = 0;
   bool tres = false;    // a helper's move is being searched again
@@ -319,6 +323,19 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
         if (!late && lane == 0) atomicOr(&args.stats->status, kErrWait);
         late = true;
         qdone = true;
+      }
+      if (args.tail_count && !late) {
+        // the queue is used up and only the slowest few positions are left:
+        // they go back to the host, which spreads each over the whole GPU
+        unsigned rest = 0xFFFFFFFFu;
+        if (lane == 0 && ld_global_volatile(&args.stats->next) >= n)
+          rest = n - ld_global_volatile(&args.stats->done);
+        rest = __shfl_sync(kFull, rest, 0);
+        if (rest <= args.tail_count) {
+          late = true;
+          qdone = true;
+          handoff = true;
+        }
       }
     }
     if (late && busy) abort = true;
@@ -355,6 +372,7 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
               atomicOr(&args.stats->status, (P & O) ? kErrOverlap : kErrDepth);
               args.score[p] = 0;
               if (args.best) args.best[p] = kMoveNoneDev;
+              atomicAdd(&args.stats->done, 1u);
             } else {
               busy = true;
               helper = false;
@@ -434,8 +452,10 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
             if (!helper) {  // the lane's own input position is solved
               if (args.nodes_out) atomicAdd(&args.nodes_out[pos], nodes);
               total_nodes += nodes;
-              args.score[pos] = static_cast<signed char>(abort ? 0 : r);
+              args.score[pos] = static_cast<signed char>(abort ? (handoff ? kUnsolvedDev : 0) : r);
               if (args.best) args.best[pos] = static_cast<signed char>(abort ? kMoveNoneDev : rootbest);
+              atomicAdd(&args.stats->done, 1u);
+              if (abort && handoff) atomicAdd(&args.stats->handed, 1u);
               busy = false;
               break;
             }

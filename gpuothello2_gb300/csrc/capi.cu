@@ -48,6 +48,12 @@ struct Context {
   size_t frames_cap = 0;
   unsigned long long* dTable = nullptr;  // transposition table
   int table_bits = 0;
+  size_t split_cap = 0;  // root split: frontier positions and their results
+  u64* dSplitP = nullptr;
+  u64* dSplitO = nullptr;
+  signed char* dSplitScore = nullptr;
+  signed char* dSplitBest = nullptr;
+  unsigned long long* dSplitNodes = nullptr;
   unsigned long long launches = 0;  // kernels launched since the context was made
 };
 
@@ -87,9 +93,22 @@ void free_buffers(Context* c) {
   c->cap = 0;
 }
 
+void free_split(Context* c) {
+  cudaFree(c->dSplitP);
+  cudaFree(c->dSplitO);
+  cudaFree(c->dSplitScore);
+  cudaFree(c->dSplitBest);
+  cudaFree(c->dSplitNodes);
+  c->dSplitP = c->dSplitO = nullptr;
+  c->dSplitScore = c->dSplitBest = nullptr;
+  c->dSplitNodes = nullptr;
+  c->split_cap = 0;
+}
+
 void free_context(Context* c) {
   cudaStreamSynchronize(c->stream);
   free_buffers(c);
+  free_split(c);
   cudaFree(c->dPerm);
   cudaFree(c->dFrontP);
   cudaFree(c->dFrontO);
@@ -146,6 +165,23 @@ int ensure_capacity(Context* c, size_t n) {
   GPO_CK(cudaMalloc(&c->dBest, cap));
   GPO_CK(cudaMalloc(&c->dNodes, cap * sizeof(unsigned long long)));
   c->cap = cap;
+  return GPO_OK;
+}
+
+// Frontier positions of a root split and their results, grown on demand;
+// apart from the caller's arrays, so that a split can finish part of a
+// batch whose outputs are still in use.
+int ensure_split(Context* c, size_t n) {
+  if (n <= c->split_cap) return GPO_OK;
+  free_split(c);
+  size_t cap = 1024;
+  while (cap < n) cap *= 2;
+  GPO_CK(cudaMalloc(&c->dSplitP, cap * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->dSplitO, cap * sizeof(u64)));
+  GPO_CK(cudaMalloc(&c->dSplitScore, cap));
+  GPO_CK(cudaMalloc(&c->dSplitBest, cap));
+  GPO_CK(cudaMalloc(&c->dSplitNodes, cap * sizeof(unsigned long long)));
+  c->split_cap = cap;
   return GPO_OK;
 }
 
@@ -227,11 +263,24 @@ constexpr int kDefaultStabGate = 10;
 constexpr int kDefaultHelpMin = 7;
 constexpr unsigned long long kDefaultHardNodes = 1ULL << 23;
 
-// Bucketing, learned root orders and the persistent search, enqueued on s;
-// waits for them and returns the status.
+int finish_tail(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+                signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
+                cudaStream_t s, gpo_stats* stats, long warps, unsigned handed);
+
+// Tail handoff (batches of DEPTH >= 14): once the queue is used up and at
+// most warps / kTailWarpsDiv positions are unfinished, the kernel hands them
+// back and a root split finishes them over the whole GPU.
+constexpr int kTailWarpsDiv = 16;
+
+// Bucketing, learned orders and the persistent search, enqueued on s; waits
+// for them and returns the status.  tail: the tail handoff is allowed (not
+// for the searches of a root split's frontier); clear_table: the
+// transposition table starts empty (a root split finishing a tail keeps the
+// entries of the search it finishes: they are exact bounds of the same
+// positions' subtrees).
 int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
-                cudaStream_t s, gpo_stats* stats) {
+                cudaStream_t s, gpo_stats* stats, bool tail, bool clear_table) {
   const int rcs = ensure_pass_scratch(c, static_cast<size_t>(n));
   if (rcs != GPO_OK) return rcs;
   GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
@@ -302,6 +351,10 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
     const long per = (n + warps - 1) / warps;
     a.roots_per_warp = static_cast<int>(per < 1 ? 1 : (per > 32 ? 32 : per));
   }
+  if (tail && depth >= 14 && o.tail_split_positions >= 0) {
+    const long cnt = o.tail_split_positions > 0 ? o.tail_split_positions : warps / kTailWarpsDiv;
+    a.tail_count = static_cast<unsigned>(cnt < n ? cnt : n);
+  }
   const size_t need = batched_gframe_bytes(depth, a.smem_top,
                                            static_cast<size_t>(cfg.grid) * cfg.threads);
   if (need > c->frames_cap) {
@@ -317,7 +370,7 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
     const int rct = ensure_table(c, bits);
     if (rct != GPO_OK) return rct;
     // cleared at every call: no result carries over from an earlier call
-    GPO_CK(cudaMemsetAsync(c->dTable, 0, static_cast<size_t>(16) << bits, s));
+    if (clear_table) GPO_CK(cudaMemsetAsync(c->dTable, 0, static_cast<size_t>(16) << bits, s));
     a.tt = c->dTable;
     a.tt_bits = bits;
     a.tt_min = o.table_min_empties > 0 ? o.table_min_empties : kDefaultTableMin;
@@ -343,7 +396,9 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
     stats->table_bits = a.tt ? a.tt_bits : 0;
     stats->kernel_ms = ms;
   }
-  return status_to_error(hs.status);
+  const int rc = status_to_error(hs.status);
+  if (rc != GPO_OK || hs.handed == 0) return rc;
+  return finish_tail(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, warps, hs.handed);
 }
 
 // ---- small batches: split at the root ----
@@ -414,24 +469,27 @@ struct SplitNode {
 // frontier size (in warps) that is enough.
 constexpr int kSplitBelowWarpsDiv = 8;
 
-int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
-                   signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
-                   cudaStream_t s, gpo_stats* stats, long warps, int plies_opt) {
-  std::vector<u64> hp(n), ho(n);
-  GPO_CK(cudaMemcpyAsync(hp.data(), dP, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
-  GPO_CK(cudaMemcpyAsync(ho.data(), dO, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
-  GPO_CK(cudaStreamSynchronize(s));
+// Root split core: the positions hp / ho (valid, at most `depth` empties)
+// are expanded on the host by at least min_plies and up to 3 plies
+// (plies_opt > 0: exactly that many) until the frontier has enough positions
+// for the GPU; the frontier is solved
+// in one batched launch and the values go back up by negamax.  Results (score,
+// best move, nodes) for each input in sc / bm / nds.
+int split_solve(Context* c, const std::vector<u64>& hp, const std::vector<u64>& ho, int depth,
+                const gpo_options& o, cudaStream_t s, long warps, int plies_opt, int min_plies,
+                bool clear_table, std::vector<signed char>& sc, std::vector<signed char>& bm,
+                std::vector<unsigned long long>& nds, gpo_stats* stats) {
+  const int n = static_cast<int>(hp.size());
   std::vector<SplitNode> t;
   t.reserve(static_cast<size_t>(n) * 64);
-  for (int i = 0; i < n; ++i) {
-    if ((hp[i] & ho[i]) || 64 - __builtin_popcountll(hp[i] | ho[i]) > depth) return 1;  // not split
-    t.push_back(SplitNode{hp[i], ho[i], -1, kMoveNoneDev, 0, 0, -1, 0, 0});
-  }
+  for (int i = 0; i < n; ++i) t.push_back(SplitNode{hp[i], ho[i], -1, kMoveNoneDev, 0, 0, -1, 0, 0});
   // expand ply by ply until the frontier has enough positions
   size_t lo = 0, hi = t.size();
   const int max_plies = plies_opt > 0 ? plies_opt : 3;
   for (int ply = 0; ply < max_plies; ++ply) {
-    if (plies_opt <= 0 && static_cast<long>(hi - lo) * kSplitBelowWarpsDiv >= warps * 4) break;
+    if (plies_opt <= 0 && ply >= min_plies &&
+        static_cast<long>(hi - lo) * kSplitBelowWarpsDiv >= warps * 4)
+      break;
     for (size_t k = lo; k < hi; ++k) {
       const u64 P = t[k].P, O = t[k].O;  // copies: push_back below may move t
       if (64 - __builtin_popcountll(P | O) <= 12) continue;  // small enough to solve whole
@@ -475,25 +533,16 @@ int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, s
   gpo_stats inner;
   std::memset(&inner, 0, sizeof(inner));
   if (m > 0) {
-    // the outputs may be the context's own staging buffers (host-buffer entry
-    // point), which growing them replaces
-    const bool staged = dScore == c->dScore;
-    int rc = ensure_capacity(c, static_cast<size_t>(m));
+    int rc = ensure_split(c, static_cast<size_t>(m));
     if (rc != GPO_OK) return rc;
-    if (staged) {
-      dScore = c->dScore;
-      if (dBest) dBest = c->dBest;
-      if (dNodes) dNodes = c->dNodes;
-    }
-    GPO_CK(cudaMemcpyAsync(c->dP, lp.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
-    GPO_CK(cudaMemcpyAsync(c->dO, lo_.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
-    rc = run_batched(c, c->dP, c->dO, m, depth, c->dScore, dBest ? c->dBest : nullptr,
-                     dNodes ? c->dNodes : nullptr, o, s, &inner);
+    GPO_CK(cudaMemcpyAsync(c->dSplitP, lp.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
+    GPO_CK(cudaMemcpyAsync(c->dSplitO, lo_.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
+    rc = run_batched(c, c->dSplitP, c->dSplitO, m, depth, c->dSplitScore, c->dSplitBest,
+                     c->dSplitNodes, o, s, &inner, false, clear_table);
     if (rc != GPO_OK) return rc;
-    GPO_CK(cudaMemcpyAsync(lsc.data(), c->dScore, m, cudaMemcpyDeviceToHost, s));
-    if (dBest) GPO_CK(cudaMemcpyAsync(lbest.data(), c->dBest, m, cudaMemcpyDeviceToHost, s));
-    if (dNodes)
-      GPO_CK(cudaMemcpyAsync(lnodes.data(), c->dNodes, m * sizeof(u64), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaMemcpyAsync(lsc.data(), c->dSplitScore, m, cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaMemcpyAsync(lbest.data(), c->dSplitBest, m, cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaMemcpyAsync(lnodes.data(), c->dSplitNodes, m * sizeof(u64), cudaMemcpyDeviceToHost, s));
     GPO_CK(cudaStreamSynchronize(s));
   }
   // negamax from the deepest nodes up (children come after their parents)
@@ -517,21 +566,95 @@ int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, s
       nd.value = best;
     }
   }
-  std::vector<signed char> sc(n), bm(n);
-  std::vector<unsigned long long> nds(n);
+  sc.resize(n);
+  bm.resize(n);
+  nds.resize(n);
   for (int i = 0; i < n; ++i) {
     sc[i] = static_cast<signed char>(t[i].value);
     bm[i] = static_cast<signed char>(bestmove[i]);
     nds[i] = t[i].nodes;
   }
-  GPO_CK(cudaMemcpyAsync(dScore, sc.data(), n, cudaMemcpyHostToDevice, s));
-  if (dBest) GPO_CK(cudaMemcpyAsync(dBest, bm.data(), n, cudaMemcpyHostToDevice, s));
-  if (dNodes) GPO_CK(cudaMemcpyAsync(dNodes, nds.data(), n * sizeof(u64), cudaMemcpyHostToDevice, s));
-  GPO_CK(cudaStreamSynchronize(s));
   if (stats) {
     *stats = inner;
     stats->nodes = inner.nodes + (t.size() - static_cast<size_t>(m));
     stats->root_split_positions = static_cast<uint64_t>(m);
+  }
+  return GPO_OK;
+}
+
+// Small batches: the whole batch goes through the root split.  Returns 1
+// without doing anything when an input must be rejected (the batched
+// kernel then reports it).
+int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+                   signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
+                   cudaStream_t s, gpo_stats* stats, long warps, int plies_opt) {
+  std::vector<u64> hp(n), ho(n);
+  GPO_CK(cudaMemcpyAsync(hp.data(), dP, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaMemcpyAsync(ho.data(), dO, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i)
+    if ((hp[i] & ho[i]) || 64 - __builtin_popcountll(hp[i] | ho[i]) > depth) return 1;
+  std::vector<signed char> sc, bm;
+  std::vector<unsigned long long> nds;
+  const int rc = split_solve(c, hp, ho, depth, o, s, warps, plies_opt, 0, true, sc, bm, nds, stats);
+  if (rc != GPO_OK) return rc;
+  GPO_CK(cudaMemcpyAsync(dScore, sc.data(), n, cudaMemcpyHostToDevice, s));
+  if (dBest) GPO_CK(cudaMemcpyAsync(dBest, bm.data(), n, cudaMemcpyHostToDevice, s));
+  if (dNodes) GPO_CK(cudaMemcpyAsync(dNodes, nds.data(), n * sizeof(u64), cudaMemcpyHostToDevice, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  return GPO_OK;
+}
+
+// Tail handoff: the `handed` positions the kernel gave back unsolved (score
+// kUnsolvedDev) are finished by a root split with the table kept, and their
+// results written into place.  Node counts add both searches.
+int finish_tail(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
+                signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
+                cudaStream_t s, gpo_stats* stats, long warps, unsigned handed) {
+  std::vector<signed char> all(static_cast<size_t>(n));
+  GPO_CK(cudaMemcpyAsync(all.data(), dScore, n, cudaMemcpyDeviceToHost, s));
+  GPO_CK(cudaStreamSynchronize(s));
+  std::vector<int> idx;
+  for (int i = 0; i < n; ++i)
+    if (all[i] == kUnsolvedDev) idx.push_back(i);
+  if (idx.size() != handed) return GPO_ERR_INTERNAL;
+  const size_t k = idx.size();
+  std::vector<u64> hp(k), ho(k);
+  std::vector<unsigned long long> first(k, 0);
+  for (size_t j = 0; j < k; ++j) {
+    GPO_CK(cudaMemcpyAsync(&hp[j], dP + idx[j], sizeof(u64), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaMemcpyAsync(&ho[j], dO + idx[j], sizeof(u64), cudaMemcpyDeviceToHost, s));
+    if (dNodes)
+      GPO_CK(cudaMemcpyAsync(&first[j], dNodes + idx[j], sizeof(u64), cudaMemcpyDeviceToHost, s));
+  }
+  GPO_CK(cudaStreamSynchronize(s));
+  std::vector<signed char> sc, bm;
+  std::vector<unsigned long long> nds;
+  gpo_stats inner;
+  std::memset(&inner, 0, sizeof(inner));
+  // the handed-back positions are the slowest of the batch: at least two
+  // plies, so that each spreads over thousands of lanes
+  const int rc = split_solve(c, hp, ho, depth, o, s, warps, 0, 2, false, sc, bm, nds, &inner);
+  if (rc != GPO_OK) return rc;
+  for (size_t j = 0; j < k; ++j) {
+    nds[j] += first[j];
+    GPO_CK(cudaMemcpyAsync(dScore + idx[j], &sc[j], 1, cudaMemcpyHostToDevice, s));
+    if (dBest) GPO_CK(cudaMemcpyAsync(dBest + idx[j], &bm[j], 1, cudaMemcpyHostToDevice, s));
+    if (dNodes)
+      GPO_CK(cudaMemcpyAsync(dNodes + idx[j], &nds[j], sizeof(u64), cudaMemcpyHostToDevice, s));
+  }
+  GPO_CK(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->nodes += inner.nodes;
+    stats->table_probes += inner.table_probes;
+    stats->table_hits += inner.table_hits;
+    stats->table_updates += inner.table_updates;
+    stats->learned_calls += inner.learned_calls;
+    stats->splits += inner.splits;
+    stats->stability_cuts += inner.stability_cuts;
+    stats->kernel_ms += inner.kernel_ms;
+    stats->root_split_positions = inner.root_split_positions;
+    stats->tail_positions = k;
   }
   return GPO_OK;
 }
@@ -575,7 +698,7 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
       if (rc != 1) return rc;  // 1: inputs the kernel must reject, solved unsplit below
     }
   }
-  return run_batched(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats);
+  return run_batched(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, true, true);
 }
 
 // ---- CUDA graphs of a batched solve (repeated batches) ----

@@ -16,6 +16,9 @@ constexpr u64 kCorners = 0x8100000000000081ULL;
 // Best-move codes (the reference's hand::PASS / hand::NOMOVE, alphabeta.cuh:7-10).
 constexpr int kMovePassDev = 64;
 constexpr int kMoveNoneDev = 65;
+// Score of a position the batched kernel handed back unsolved (tail handoff):
+// outside every real score's range [-64, 64].
+constexpr int kUnsolvedDev = -128;
 
 // Error bits set by kernels in the device status word (host maps them to
 // the negative GPO_ERR_* codes of the C-ABI).
@@ -39,6 +42,8 @@ struct DeviceStats {
   unsigned long long stab_cuts;  // nodes closed by the stability cutoff
   unsigned int status;
   unsigned int next;             // work-queue cursor of the persistent kernel
+  unsigned int done;             // input positions finished (solved, rejected or handed back)
+  unsigned int handed;           // input positions handed back unsolved (tail handoff)
   unsigned long long t0;         // plain kernel: global timer at its first block's start
 };
 

@@ -52,6 +52,11 @@ struct BatchedArgs {
   int learned_min;
   unsigned long long node_budget;    // per input position, 0 = none (watchdog)
   unsigned long long wait_limit_ns;  // deadline of the launch, from its start
+  // Tail handoff: once the queue is used up and at most tail_count input
+  // positions are unfinished, every search stops and its position's score
+  // is kUnsolvedDev, for the host to solve spread over the whole GPU
+  // (0 = off).
+  unsigned tail_count;
 };
 
 struct BatchedLaunch {

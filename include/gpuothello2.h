@@ -93,6 +93,11 @@ typedef struct gpo_options {
                                  are not expanded), every frontier position solved exactly in
                                  one launch, values taken back up by negamax; > 0 = always
                                  expand this many plies; negative = never */
+  int tail_split_positions;   /* tail handoff (depth >= 14): once every position has been
+                                 taken up and at most this many are unfinished, their
+                                 searches stop and a root split finishes them over the whole
+                                 GPU, the table kept; 0 = default (1/16 of the GPU's warps),
+                                 negative = off */
 } gpo_options;
 
 typedef struct gpo_stats {
@@ -108,6 +113,7 @@ typedef struct gpo_stats {
   uint64_t stability_cuts; /* nodes closed by the stability cutoff */
   uint64_t table_bits;     /* log2 of the table's entries used by the call (0 = no table) */
   uint64_t root_split_positions; /* frontier positions a root split solved (0 = no split) */
+  uint64_t tail_positions; /* positions finished by the tail handoff's root split */
 } gpo_stats;
 
 /* Fills *opt with the defaults (all fields "auto"/0). */

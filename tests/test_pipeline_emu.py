@@ -108,6 +108,21 @@ def test_root_split_of_small_batches(emu, oracle, plies):
     assert rc == 0 and np.array_equal(sc2, want) and st2.root_split_positions == 0
 
 
+def test_tail_handoff(emu, oracle):
+    """Once the queue is used up and few positions are unfinished, the
+    kernel hands them back unsolved and a root split finishes them with the
+    table kept: scores, best moves and node totals as without it."""
+    p, o = oracle.generate(14, 12, 13, 14)
+    want, _, _, _ = oracle.solve_batch(p, o, mode=1)
+    rc, sc, bm, nodes, st = solve(emu, p, o, 14, tail_split_positions=4, root_split_plies=-1)
+    assert rc == 0 and np.array_equal(sc, want)
+    assert 1 <= st.tail_positions <= 4 and st.root_split_positions > st.tail_positions
+    assert st.nodes == int(nodes.sum())
+    best_moves_reach_scores(oracle, p, o, sc, bm)
+    rc, sc2, _, _, st2 = solve(emu, p, o, 14, tail_split_positions=-1, root_split_plies=-1)
+    assert rc == 0 and np.array_equal(sc2, want) and st2.tail_positions == 0
+
+
 def test_mixed_empties_without_shared_frames(emu):
     p, o, scores, _ = golden_ref("c3_seed2_mixed")
     small = (64 - np.array([bin(int(a) | int(b)).count("1") for a, b in zip(p, o)])) <= 11
@@ -198,5 +213,7 @@ def test_random_option_mixes(emu, oracle):
             kw["smem_frames"] = int(rng.choice([-1, 1, 3, 8]))
         if rng.random() < 0.3:
             kw["fastest_first_empties"] = int(rng.integers(3, 13))
+        if rng.random() < 0.3:
+            kw["tail_split_positions"] = int(rng.choice([-1, 2, 5]))
         rc, sc, _, _, _ = solve(emu, p, o, depth, **kw)
         assert rc == 0 and np.array_equal(sc, want), (n, lo, hi, depth, kw)
