@@ -75,7 +75,7 @@ def test_training_learns_best_moves(gpu, oracle):
     assert acc1 > acc0 + 0.1
 
 
-def test_learned_root_order_keeps_scores_exact(gpu):
+def test_learned_order_keeps_scores_exact(gpu):
     p, o, best = labelled(gpu, 3, 32768, 12, 14)
     w, _ = gpu.mlp_train(p, o, best, gpu.mlp_init(5), epochs=3, batch=2048, lr=1e-3, seed=2)
     q, r = gpu.generate(4, 2048, 14, 16)
@@ -86,6 +86,8 @@ def test_learned_root_order_keeps_scores_exact(gpu):
     finally:
         gpu.mlp_load(None)
     assert np.array_equal(s0, s1)
-    assert st1.learned_calls == len(q)
-    print("nodes: fastest-first roots %d, learned roots %d (%.3f)" %
-          (st0.nodes, st1.nodes, st1.nodes / st0.nodes))
+    # the network scores every node with >= 14 empties in the top two plies
+    # of each position: at least the positions themselves
+    assert st0.learned_calls == 0 and st1.learned_calls >= len(q)
+    print("nodes: fastest-first %d, learned %d (%.3f), %d positions scored" %
+          (st0.nodes, st1.nodes, st1.nodes / st0.nodes, st1.learned_calls))
