@@ -26,7 +26,7 @@ the timed region.
 The transposition table is always on; the line reports its size, probes,
 hits, updates and 32-byte-sector traffic rate.  A stratified sample of the
 scores is checked against the oracle outside the timed region
-(`parity_sample`).  The top of the search (nodes with >= 14 empties in the
+(`parity_sample`).  The top of the search (nodes with >= 12 empties in the
 first two plies) is ordered by the learned move orderer, whose weights were
 trained by the library's own GPU kernels and are loaded from a file
 (`--no-learned`: fastest-first only).  Options: `--tuned` autotunes the launch and search parameters on
@@ -339,7 +339,7 @@ def main():
     if args.learned:
         w = np.fromfile(args.weights, dtype=np.float32)
         g.mlp_load(w)
-        learned_info = {"weights": os.path.relpath(args.weights, ROOT), "min_empties": 14}
+        learned_info = {"weights": os.path.relpath(args.weights, ROOT), "min_empties": 12}
     tuned, tuned_src = {}, None
     if args.tuned:
         from gpuothello2_gb300 import autotune

@@ -262,6 +262,9 @@ constexpr int kDefaultStabMin = 4;
 constexpr int kDefaultStabGate = 10;
 constexpr int kDefaultHelpMin = 7;
 constexpr unsigned long long kDefaultHardNodes = 1ULL << 23;
+// Learned ordering at the top two plies' nodes with >= 12 empties (the
+// network was trained on positions with 12-14 empties).
+constexpr int kDefaultLearnedMin = 12;
 
 int finish_tail(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
@@ -290,7 +293,7 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   // Learned ordering for the positions with >= learned_min empties (the
   // front of the bucketed queue): the network scores the top two plies of
   // their trees ahead of the search (mlp_order_frontier).
-  const int lmin = o.learned_min_empties > 0 ? o.learned_min_empties : 14;
+  const int lmin = o.learned_min_empties > 0 ? o.learned_min_empties : kDefaultLearnedMin;
   const bool learned = (o.use_learned > 0 || (o.use_learned < 0 && mlp_loaded())) && depth >= lmin;
   long learned_count = 0, frontier = 0;
   if (learned) {

@@ -65,7 +65,7 @@ typedef struct gpo_options {
   int fastest_first_empties;  /* fastest-first ordering at nodes with >= this many empties;
                                  0 = default (6) */
   int learned_min_empties;    /* learned ordering at the nodes with >= this many empties in
-                                 the top two plies of each position; 0 = 14 */
+                                 the top two plies of each position; 0 = 12 */
   uint64_t node_budget;       /* per-position node limit, 0 = none (watchdog: GPO_ERR_TIMEOUT) */
   int help_min_empties;       /* idle lanes of a warp help its busy lanes with moves of nodes
                                  that have >= this many empties (young brothers wait, after
