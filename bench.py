@@ -58,7 +58,8 @@ W_NODE = 418  # INT32 ops per node: mobility + flip + make-move of the reference
 # the traffic is the transposition table's, which grows with the nodes.
 TRAFFIC_BYTES_PER_NODE = (6.700996e9 + 3.144086e9) / 3303996693
 TRAFFIC_SOURCE = ("ncu capture of 131,072 positions x 12 empties (9.85 GB in 3.30e9 nodes, "
-                  "profiles/batched_kernel_ncu.md), scaled by nodes")
+                  "profiles/batched_kernel_ncu.md; table from 7 empties there, from 9 now, "
+                  "so an upper estimate), scaled by nodes")
 SEED, N_POS, LO, HI, DEPTH = 2, 1 << 20, 8, 16, 16
 METRIC = "exact-solved positions/s at 8\u201316 empties: batched+learned vs plain, same GB300"
 WORKLOAD = ("1,048,576 positions, random playouts seed 2, empties uniform 8..16, DEPTH 16")
@@ -431,7 +432,7 @@ def main():
                    "hits": sum(st.table_hits for st in stats), "updates": updates,
                    "sector_bytes": 32 * (probes + 2 * updates),
                    "gbs": 32 * (probes + 2 * updates) / kern_s / 1e9 if kern_s > 0 else None,
-                   "min_empties": 7}
+                   "min_empties": 9}
 
     plain = None
     if args.plain:

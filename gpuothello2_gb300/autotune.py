@@ -35,7 +35,7 @@ DEFAULTS = {
     "threads_per_block": 128,
     "smem_frames": 0,
     "fastest_first_empties": 6,
-    "table_min_empties": 7,
+    "table_min_empties": 9,
     "help_min_empties": 7,
 }
 

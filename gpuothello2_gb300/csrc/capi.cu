@@ -246,10 +246,10 @@ int check_options(const gpo_options* opt) {
 }
 
 // Defaults of the batched search (the autotuner can choose others per GPU):
-// fastest-first from 6 empties, table from 7, the stability cutoff from 4
+// fastest-first from 6 empties, table from 9, the stability cutoff from 4
 // empties when alpha >= 10 + 3 * empties, helping from 7.
 constexpr int kDefaultFF = 6;
-constexpr int kDefaultTableMin = 7;
+constexpr int kDefaultTableMin = 9;
 // Table size: tens of thousands of searches run at once and share it, so
 // it pays to give it real capacity: 2^28 entries (4 GiB) on a device with
 // at least 64 GiB, else 2^24 (256 MiB).

@@ -74,7 +74,7 @@ typedef struct gpo_options {
   int table_bits;             /* transposition table of 2^table_bits 16-byte entries in
                                  buckets of two (17..32); 0 = 28 (4 GiB) on a device with
                                  >= 64 GiB of memory, else 24 (256 MiB) */
-  int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 7 */
+  int table_min_empties;      /* nodes with >= this many empties use the table; 0 = 9 */
   int smem_frames;            /* search frames (depth - 2 slots per lane) in shared memory:
                                  0 = when they all fit at the register-limited occupancy,
                                  > 0 = only if at most this many are needed, negative = never
