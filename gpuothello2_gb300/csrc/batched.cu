@@ -335,6 +335,20 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
           late = true;
           qdone = true;
           handoff = true;
+          if (args.tail_bound && busy && !helper) {
+            // what the root knows: its completed moves' best value (a lower
+            // bound of its score), from its own registers or its frame
+            int lb = -65;
+            if (E == root_e) {
+              if (!passed) lb = best;
+            } else {
+              u64 m0, f0;
+              unsigned x0;
+              fr.load(root_e, m0, f0, x0);
+              if (!meta_passed(x0)) lb = meta_best(x0);
+            }
+            args.tail_bound[pos] = static_cast<signed char>(lb);
+          }
         }
       }
     }
@@ -377,8 +391,8 @@ __global__ void __launch_bounds__(GPO_BATCHED_MIN_BLOCKS > 1 ? 128 : 256, GPO_BA
               busy = true;
               helper = false;
               pos = p;
-              alpha = -64;
-              beta = 64;
+              alpha = args.root_window ? args.root_window[2 * p] : -64;
+              beta = args.root_window ? args.root_window[2 * p + 1] : 64;
               phase = PH_INIT;
               root_e = E;
               P0 = P;

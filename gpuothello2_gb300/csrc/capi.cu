@@ -54,6 +54,9 @@ struct Context {
   signed char* dSplitScore = nullptr;
   signed char* dSplitBest = nullptr;
   unsigned long long* dSplitNodes = nullptr;
+  signed char* dSplitWin = nullptr;  // frontier windows (alpha, beta)
+  size_t bound_cap = 0;  // tail handoff: the roots' lower bounds
+  signed char* dBound = nullptr;
   unsigned long long launches = 0;  // kernels launched since the context was made
 };
 
@@ -99,8 +102,9 @@ void free_split(Context* c) {
   cudaFree(c->dSplitScore);
   cudaFree(c->dSplitBest);
   cudaFree(c->dSplitNodes);
+  cudaFree(c->dSplitWin);
   c->dSplitP = c->dSplitO = nullptr;
-  c->dSplitScore = c->dSplitBest = nullptr;
+  c->dSplitScore = c->dSplitBest = c->dSplitWin = nullptr;
   c->dSplitNodes = nullptr;
   c->split_cap = 0;
 }
@@ -109,6 +113,7 @@ void free_context(Context* c) {
   cudaStreamSynchronize(c->stream);
   free_buffers(c);
   free_split(c);
+  cudaFree(c->dBound);
   cudaFree(c->dPerm);
   cudaFree(c->dFrontP);
   cudaFree(c->dFrontO);
@@ -181,7 +186,20 @@ int ensure_split(Context* c, size_t n) {
   GPO_CK(cudaMalloc(&c->dSplitScore, cap));
   GPO_CK(cudaMalloc(&c->dSplitBest, cap));
   GPO_CK(cudaMalloc(&c->dSplitNodes, cap * sizeof(unsigned long long)));
+  GPO_CK(cudaMalloc(&c->dSplitWin, 2 * cap));
   c->split_cap = cap;
+  return GPO_OK;
+}
+
+int ensure_bound(Context* c, size_t n) {
+  if (n <= c->bound_cap) return GPO_OK;
+  cudaFree(c->dBound);
+  c->dBound = nullptr;
+  c->bound_cap = 0;
+  size_t cap = 1024;
+  while (cap < n) cap *= 2;
+  GPO_CK(cudaMalloc(&c->dBound, cap));
+  c->bound_cap = cap;
   return GPO_OK;
 }
 
@@ -268,7 +286,8 @@ constexpr int kDefaultLearnedMin = 12;
 
 int finish_tail(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
-                cudaStream_t s, gpo_stats* stats, long warps, unsigned handed);
+                cudaStream_t s, gpo_stats* stats, long warps, unsigned handed,
+                const signed char* dBound);
 
 // Tail handoff (batches of DEPTH >= 14): once the queue is used up and at
 // most warps / kTailWarpsDiv positions are unfinished, the kernel hands them
@@ -280,10 +299,11 @@ constexpr int kTailWarpsDiv = 16;
 // for the searches of a root split's frontier); clear_table: the
 // transposition table starts empty (a root split finishing a tail keeps the
 // entries of the search it finishes: they are exact bounds of the same
-// positions' subtrees).
+// positions' subtrees); dWin: per-position root windows, or null.
 int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
-                cudaStream_t s, gpo_stats* stats, bool tail, bool clear_table) {
+                cudaStream_t s, gpo_stats* stats, bool tail, bool clear_table,
+                const signed char* dWin) {
   const int rcs = ensure_pass_scratch(c, static_cast<size_t>(n));
   if (rcs != GPO_OK) return rcs;
   GPO_CK(cudaMemsetAsync(c->dStats, 0, sizeof(DeviceStats), s));
@@ -357,7 +377,13 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   if (tail && depth >= 14 && o.tail_split_positions >= 0) {
     const long cnt = o.tail_split_positions > 0 ? o.tail_split_positions : warps / kTailWarpsDiv;
     a.tail_count = static_cast<unsigned>(cnt < n ? cnt : n);
+    if (a.tail_count > 0) {
+      const int rcb = ensure_bound(c, static_cast<size_t>(n));
+      if (rcb != GPO_OK) return rcb;
+      a.tail_bound = c->dBound;
+    }
   }
+  a.root_window = dWin;
   const size_t need = batched_gframe_bytes(depth, a.smem_top,
                                            static_cast<size_t>(cfg.grid) * cfg.threads);
   if (need > c->frames_cap) {
@@ -401,7 +427,8 @@ int run_batched(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   }
   const int rc = status_to_error(hs.status);
   if (rc != GPO_OK || hs.handed == 0) return rc;
-  return finish_tail(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, warps, hs.handed);
+  return finish_tail(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, warps, hs.handed,
+                     c->dBound);
 }
 
 // ---- small batches: split at the root ----
@@ -475,13 +502,23 @@ constexpr int kSplitBelowWarpsDiv = 8;
 // Root split core: the positions hp / ho (valid, at most `depth` empties)
 // are expanded on the host by at least min_plies and up to 3 plies
 // (plies_opt > 0: exactly that many) until the frontier has enough positions
-// for the GPU; the frontier is solved
-// in one batched launch and the values go back up by negamax.  Results (score,
-// best move, nodes) for each input in sc / bm / nds.
+// for the GPU; the frontier is solved in one batched launch and the values go
+// back up by negamax.  Results (score, best move, nodes) for each input in
+// sc / bm / nds.
+//
+// lb (optional): a known lower bound L of each input's score (-65 = none).
+// Only the frontier values that can decide a score >= L are then needed
+// exactly: a frontier position an even number of plies below its root is
+// searched with the window (L - 1, 64), one an odd number below with
+// (-64, 1 - L).  A move whose subtree holds a value outside its window is
+// worth at most L - 1 to the root, below the score; the move that makes the
+// score has every value of its subtree inside the windows, so negamax over
+// the fail-soft results still gives the exact score and a best move.
 int split_solve(Context* c, const std::vector<u64>& hp, const std::vector<u64>& ho, int depth,
                 const gpo_options& o, cudaStream_t s, long warps, int plies_opt, int min_plies,
-                bool clear_table, std::vector<signed char>& sc, std::vector<signed char>& bm,
-                std::vector<unsigned long long>& nds, gpo_stats* stats) {
+                bool clear_table, const std::vector<int>* lb, std::vector<signed char>& sc,
+                std::vector<signed char>& bm, std::vector<unsigned long long>& nds,
+                gpo_stats* stats) {
   const int n = static_cast<int>(hp.size());
   std::vector<SplitNode> t;
   t.reserve(static_cast<size_t>(n) * 64);
@@ -533,6 +570,29 @@ int split_solve(Context* c, const std::vector<u64>& hp, const std::vector<u64>& 
   const int m = static_cast<int>(lp.size());
   std::vector<signed char> lsc(m), lbest(m, kMoveNoneDev);
   std::vector<unsigned long long> lnodes(m, 0);
+  std::vector<signed char> win;
+  if (lb) {
+    win.resize(2 * static_cast<size_t>(m));
+    for (size_t k = 0; k < t.size(); ++k) {
+      if (t[k].leaf < 0) continue;
+      int root = static_cast<int>(k), plies = 0;
+      while (t[root].parent >= 0) {
+        root = t[root].parent;
+        ++plies;
+      }
+      const int L = (*lb)[root];
+      int a = -64, b = 64;
+      if (L > -63 && L <= 64) {
+        if (plies & 1) {
+          b = 1 - L;
+        } else {
+          a = L - 1;
+        }
+      }
+      win[2 * t[k].leaf] = static_cast<signed char>(a);
+      win[2 * t[k].leaf + 1] = static_cast<signed char>(b);
+    }
+  }
   gpo_stats inner;
   std::memset(&inner, 0, sizeof(inner));
   if (m > 0) {
@@ -540,8 +600,10 @@ int split_solve(Context* c, const std::vector<u64>& hp, const std::vector<u64>& 
     if (rc != GPO_OK) return rc;
     GPO_CK(cudaMemcpyAsync(c->dSplitP, lp.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
     GPO_CK(cudaMemcpyAsync(c->dSplitO, lo_.data(), m * sizeof(u64), cudaMemcpyHostToDevice, s));
+    if (lb) GPO_CK(cudaMemcpyAsync(c->dSplitWin, win.data(), 2 * m, cudaMemcpyHostToDevice, s));
     rc = run_batched(c, c->dSplitP, c->dSplitO, m, depth, c->dSplitScore, c->dSplitBest,
-                     c->dSplitNodes, o, s, &inner, false, clear_table);
+                     c->dSplitNodes, o, s, &inner, false, clear_table,
+                     lb ? c->dSplitWin : nullptr);
     if (rc != GPO_OK) return rc;
     GPO_CK(cudaMemcpyAsync(lsc.data(), c->dSplitScore, m, cudaMemcpyDeviceToHost, s));
     GPO_CK(cudaMemcpyAsync(lbest.data(), c->dSplitBest, m, cudaMemcpyDeviceToHost, s));
@@ -599,7 +661,8 @@ int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, s
     if ((hp[i] & ho[i]) || 64 - __builtin_popcountll(hp[i] | ho[i]) > depth) return 1;
   std::vector<signed char> sc, bm;
   std::vector<unsigned long long> nds;
-  const int rc = split_solve(c, hp, ho, depth, o, s, warps, plies_opt, 0, true, sc, bm, nds, stats);
+  const int rc =
+      split_solve(c, hp, ho, depth, o, s, warps, plies_opt, 0, true, nullptr, sc, bm, nds, stats);
   if (rc != GPO_OK) return rc;
   GPO_CK(cudaMemcpyAsync(dScore, sc.data(), n, cudaMemcpyHostToDevice, s));
   if (dBest) GPO_CK(cudaMemcpyAsync(dBest, bm.data(), n, cudaMemcpyHostToDevice, s));
@@ -613,7 +676,8 @@ int run_root_split(Context* c, const u64* dP, const u64* dO, int n, int depth, s
 // results written into place.  Node counts add both searches.
 int finish_tail(Context* c, const u64* dP, const u64* dO, int n, int depth, signed char* dScore,
                 signed char* dBest, unsigned long long* dNodes, const gpo_options& o,
-                cudaStream_t s, gpo_stats* stats, long warps, unsigned handed) {
+                cudaStream_t s, gpo_stats* stats, long warps, unsigned handed,
+                const signed char* dBound) {
   std::vector<signed char> all(static_cast<size_t>(n));
   GPO_CK(cudaMemcpyAsync(all.data(), dScore, n, cudaMemcpyDeviceToHost, s));
   GPO_CK(cudaStreamSynchronize(s));
@@ -624,20 +688,24 @@ int finish_tail(Context* c, const u64* dP, const u64* dO, int n, int depth, sign
   const size_t k = idx.size();
   std::vector<u64> hp(k), ho(k);
   std::vector<unsigned long long> first(k, 0);
+  std::vector<signed char> bound(k, -65);
   for (size_t j = 0; j < k; ++j) {
     GPO_CK(cudaMemcpyAsync(&hp[j], dP + idx[j], sizeof(u64), cudaMemcpyDeviceToHost, s));
     GPO_CK(cudaMemcpyAsync(&ho[j], dO + idx[j], sizeof(u64), cudaMemcpyDeviceToHost, s));
     if (dNodes)
       GPO_CK(cudaMemcpyAsync(&first[j], dNodes + idx[j], sizeof(u64), cudaMemcpyDeviceToHost, s));
+    GPO_CK(cudaMemcpyAsync(&bound[j], dBound + idx[j], 1, cudaMemcpyDeviceToHost, s));
   }
   GPO_CK(cudaStreamSynchronize(s));
+  // the stopped searches' lower bounds narrow the frontier's windows
+  const std::vector<int> lb(bound.begin(), bound.end());
   std::vector<signed char> sc, bm;
   std::vector<unsigned long long> nds;
   gpo_stats inner;
   std::memset(&inner, 0, sizeof(inner));
   // the handed-back positions are the slowest of the batch: at least two
   // plies, so that each spreads over thousands of lanes
-  const int rc = split_solve(c, hp, ho, depth, o, s, warps, 0, 2, false, sc, bm, nds, &inner);
+  const int rc = split_solve(c, hp, ho, depth, o, s, warps, 0, 2, false, &lb, sc, bm, nds, &inner);
   if (rc != GPO_OK) return rc;
   for (size_t j = 0; j < k; ++j) {
     nds[j] += first[j];
@@ -701,7 +769,7 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
       if (rc != 1) return rc;  // 1: inputs the kernel must reject, solved unsplit below
     }
   }
-  return run_batched(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, true, true);
+  return run_batched(c, dP, dO, n, depth, dScore, dBest, dNodes, o, s, stats, true, true, nullptr);
 }
 
 // ---- CUDA graphs of a batched solve (repeated batches) ----

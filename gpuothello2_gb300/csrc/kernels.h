@@ -57,6 +57,13 @@ struct BatchedArgs {
   // is kUnsolvedDev, for the host to solve spread over the whole GPU
   // (0 = off).
   unsigned tail_count;
+  // Per input position, the root's lower bound when it was handed back: the
+  // best value of its completed moves (-65 = none yet); null = not wanted.
+  signed char* tail_bound;
+  // Per input position, the root's window (alpha, beta); null = (-64, 64).
+  // A root searched with a window gets a fail-soft score: exact inside the
+  // window, a bound outside it.
+  const signed char* root_window;
 };
 
 struct BatchedLaunch {
