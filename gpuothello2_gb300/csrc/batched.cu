@@ -26,7 +26,9 @@
 //   - a move at a node with two empties scores its child (one empty) in the
 //     same step: the child's last move needs only a flip count;
 //   - passes happen in place with the window negated and swapped
-//     (solver.cu:57-73, 214-221, 246-256 semantics).
+//     (solver.cu:57-73, 214-221, 246-256 semantics); the position after
+//     the pass is a node of its own for the table and the stability cutoff
+//     (in a lopsided game one side passes again and again).
 //
 // Uniform step.  Every loop iteration every lane does at most one move flip
 // plus one mobility (or, at nodes with two empties, the child's last-square
@@ -61,6 +63,14 @@
 // abandon their subtrees.  Helpers may split their own nodes in turn.  All
 // waiting is between lanes of one warp inside one loop, so it always ends;
 // a launch deadline still bounds everything.
+//
+// Tail handoff.  Once the queue is used up and at most tail_count positions
+// are unfinished, every warp stops its searches the way the deadline does
+// (without the error): each stopped position gets the score kUnsolvedDev and
+// its root's lower bound (the best value of its completed moves), and the
+// host finishes them with a root split over the whole GPU.  Roots may carry
+// windows (root_window): the root split searches its frontier with windows
+// derived from those bounds.
 #include "common.cuh"
 #include "kernels.h"
 #include "search.cuh"

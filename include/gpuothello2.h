@@ -96,8 +96,9 @@ typedef struct gpo_options {
   int tail_split_positions;   /* tail handoff (depth >= 14): once every position has been
                                  taken up and at most this many are unfinished, their
                                  searches stop and a root split finishes them over the whole
-                                 GPU, the table kept; 0 = default (1/16 of the GPU's warps),
-                                 negative = off */
+                                 GPU, the table kept and the frontier searched with windows
+                                 from what the stopped searches proved; 0 = default (1/16 of
+                                 the GPU's warps), negative = off */
 } gpo_options;
 
 typedef struct gpo_stats {
