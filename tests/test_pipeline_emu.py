@@ -108,19 +108,27 @@ def test_root_split_of_small_batches(emu, oracle, plies):
     assert rc == 0 and np.array_equal(sc2, want) and st2.root_split_positions == 0
 
 
-def test_tail_handoff(emu, oracle):
+@pytest.mark.parametrize("seed,n,lo,tail,kw", [(14, 12, 13, 4, {}),
+                                                (15, 9, 12, 6, {"threads_per_block": 64}),
+                                                (16, 11, 12, 3, {"roots_per_warp": 2})])
+def test_tail_handoff(emu, oracle, seed, n, lo, tail, kw):
     """Once the queue is used up and few positions are unfinished, the
-    kernel hands them back unsolved and a root split finishes them with the
-    table kept: scores, best moves and node totals as without it."""
-    p, o = oracle.generate(14, 12, 13, 14)
+    kernel hands them back unsolved, each with its root's lower bound, and a
+    root split finishes them with the table kept and the frontier searched
+    in windows from those bounds: scores, best moves and node totals as
+    without it."""
+    p, o = oracle.generate(seed, n, lo, 14)
     want, _, _, _ = oracle.solve_batch(p, o, mode=1)
-    rc, sc, bm, nodes, st = solve(emu, p, o, 14, tail_split_positions=4, root_split_plies=-1)
+    rc, sc, bm, nodes, st = solve(emu, p, o, 14, tail_split_positions=tail, root_split_plies=-1,
+                                  **kw)
     assert rc == 0 and np.array_equal(sc, want)
-    assert 1 <= st.tail_positions <= 4 and st.root_split_positions > st.tail_positions
+    # (positions with <= 12 empties go to the frontier unexpanded)
+    assert 1 <= st.tail_positions <= tail and st.root_split_positions >= st.tail_positions
     assert st.nodes == int(nodes.sum())
     best_moves_reach_scores(oracle, p, o, sc, bm)
-    rc, sc2, _, _, st2 = solve(emu, p, o, 14, tail_split_positions=-1, root_split_plies=-1)
-    assert rc == 0 and np.array_equal(sc2, want) and st2.tail_positions == 0
+    if seed == 14:
+        rc, sc2, _, _, st2 = solve(emu, p, o, 14, tail_split_positions=-1, root_split_plies=-1)
+        assert rc == 0 and np.array_equal(sc2, want) and st2.tail_positions == 0
 
 
 def test_mixed_empties_without_shared_frames(emu):
