@@ -19,6 +19,12 @@ reference's ascending (player, opponent) order, from `refsolve --per-board`):
                              DEPTH 22
   readme9.txt / .ref         the 9 board lines shown in the reference
                              README (README.md:11-19), DEPTH 10
+  lop_seed21_e11_12.txt/.ref 48 lopsided positions of seed 21 (11..12
+                             empties): the first whose score the oracle's
+                             alpha-beta puts at |score| >= 40 in under
+                             100,000 nodes (games where one side passes
+                             again and again), DEPTH 12; the scores in the
+                             .ref file are the reference's own
   codec_vectors.txt          2,000 random disjoint boards encoded by the
                              reference's fromBoard ("<p hex> <o hex> <str>")
 
@@ -99,6 +105,25 @@ def generate_lines(lib, seed, count, lo, hi):
     return out
 
 
+def lopsided_lines(lib, seed, lo, hi, count):
+    """The first `count` positions of the stream whose score the oracle's
+    alpha-beta puts at |score| >= 40 within 100,000 nodes (selection only;
+    the fixture's scores come from the reference)."""
+    from tests.oracle_lib import Oracle
+    from gpuothello2_gb300 import build as B
+
+    orc = Oracle(B.ORACLE_LIB)
+    p, o = orc.generate(seed, 20000, lo, hi)
+    sc, _, nodes, _ = orc.solve_batch(p, o, mode=1)
+    pick = np.nonzero((np.abs(sc.astype(int)) >= 40) & (nodes < 100000))[0][:count]
+    buf = ctypes.create_string_buffer(17)
+    out = []
+    for i in pick:
+        lib.orc_encode(int(p[i]), int(o[i]), buf)
+        out.append(buf.value.decode())
+    return out
+
+
 def run_reference(refsolve, lines, depth, jobs, prefix=()):
     """Runs the reference per board on `jobs` processes; returns its lines
     re-sorted into the reference's (player, opponent) order.  `prefix` goes
@@ -141,6 +166,13 @@ def main():
         with open(os.path.join(HERE, name + ".ref"), "w") as f:
             f.write("\n".join(ref) + "\n")
         print(name, len(lines), "boards,", len(ref), "unique")
+    if not want or "lop_seed21_e11_12" in want:
+        lines = lopsided_lines(lib, 21, 11, 12, 48)
+        write_boards(os.path.join(HERE, "lop_seed21_e11_12.txt"), lines)
+        ref = run_reference(refsolve, lines, 12, args.jobs)
+        with open(os.path.join(HERE, "lop_seed21_e11_12.ref"), "w") as f:
+            f.write("\n".join(ref) + "\n")
+        print("lop_seed21_e11_12", len(lines), "boards,", len(ref), "unique")
     if not want or "readme9" in want:
         readme = open("/root/reference/README.md").read().splitlines()
         lines = [ln.strip() for ln in readme[10:19]]

@@ -93,17 +93,15 @@ def test_stability_cutoff(emu, c1):
     assert st[5] > 0  # nodes closed by the cutoff
 
 
-def test_lopsided_positions_with_passes(emu, oracle):
+def test_lopsided_positions_with_passes(emu):
     """Lopsided endgames (|score| >= 40), where one side passes again and
-    again: the position after a pass is probed in the table, recorded and
-    tried for the stability cutoff like any created node."""
-    p, o = oracle.generate(21, 4000, 11, 12)
-    want, _, onodes, _ = oracle.solve_batch(p, o, mode=1)
-    pick = np.nonzero((np.abs(want.astype(int)) >= 40) & (onodes < 50000))[0][:16]
-    p, o, want = p[pick], o[pick], want[pick]
-    sc, _, nodes, st = emu(p, o, 12, shared_frames=1, tt_bits=17, tt_min=5, stab_min=4,
-                           stab_gate=-64)
-    assert np.array_equal(sc, want) and st[6] == 0
+    again, against the reference's own scores: the position after a pass is
+    probed in the table, recorded and tried for the stability cutoff like
+    any created node."""
+    p, o, want, _ = golden_ref("lop_seed21_e11_12")
+    sc, _, nodes, st = emu(p, o, 12, warps=2, shared_frames=1, tt_bits=17, tt_min=5,
+                           stab_min=4, stab_gate=-64)
+    assert np.array_equal(sc.astype(int), want) and st[6] == 0
     assert st[1] > 0 and st[5] > 0  # table probes, stability cutoffs
 
 

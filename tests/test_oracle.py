@@ -101,6 +101,16 @@ def test_readme_boards(oracle):
     assert codec.decode("!!%[nNNNNNnNNNNN") == (0xfffff7fffff78300, 0x0000080000087000)
 
 
+def test_lopsided_boards(oracle):
+    """Lopsided endgames where one side passes again and again: the oracle
+    walks the reference's tree on them too (scores and loop-step counts)."""
+    p, o, scores, steps = golden_ref("lop_seed21_e11_12")
+    assert (np.abs(scores) >= 40).all()
+    sc, st, _, _ = oracle.solve_batch(p, o, 12, mode=0)
+    assert np.array_equal(sc.astype(int), scores)
+    assert np.array_equal(st, steps)
+
+
 def test_codec_matches_reference_vectors(oracle):
     path = os.path.join(GOLDEN, "codec_vectors.txt")
     n = 0
