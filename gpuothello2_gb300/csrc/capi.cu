@@ -773,9 +773,9 @@ int run_solve(Context* c, const u64* dP, const u64* dO, int n, int depth, signed
 }
 
 // ---- CUDA graphs of a batched solve (repeated batches) ----
-// The batched path without the learned ordering or the root split is a
-// fixed sequence of stream work: clear the counters, bucket, clear the
-// table, search, copy the counters out.  For a caller that solves batch
+// The batched path without the learned ordering, the root split or the tail
+// handoff is a fixed sequence of stream work: clear the counters, bucket,
+// clear the table, search, copy the counters out.  For a caller that solves batch
 // after batch in the same device arrays, that sequence is captured once into
 // a CUDA graph and replayed: one graph launch instead of seven API calls
 // and launches, and no host work between them.  The graph owns every buffer

@@ -172,8 +172,9 @@ int gpo_generate_device(uint64_t seed, uint64_t first, int n, int min_empties, i
  * size in the same device arrays can instead capture the batched solve once
  * and replay it.  gpo_graph_create captures the solve of n positions held in
  * d_player/d_opp (scores to d_score) with the given options (NULL =
- * defaults; the learned ordering and the root split of small batches need
- * host decisions and are left out: use_learned must not be 1); the graph owns
+ * defaults; the learned ordering, the root split of small batches and the
+ * tail handoff need host decisions and are left out: use_learned must not be
+ * 1); the graph owns
  * its scratch and table.  gpo_graph_launch replays it on `stream` (NULL =
  * the legacy default stream) and returns at once: refill the inputs in place
  * between replays, ordered on the same stream.  gpo_graph_stats, after the
