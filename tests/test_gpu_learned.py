@@ -91,3 +91,26 @@ def test_learned_order_keeps_scores_exact(gpu):
     assert st0.learned_calls == 0 and st1.learned_calls >= len(q)
     print("nodes: fastest-first %d, learned %d (%.3f), %d positions scored" %
           (st0.nodes, st1.nodes, st1.nodes / st0.nodes, st1.learned_calls))
+
+
+def test_shipped_weights_cut_nodes(gpu):
+    """The committed weights (gpuothello2_gb300/data/orderer.f32) order the
+    search better than fastest-first: on a fixed set of 16-empty positions
+    the node count falls (about 16% on larger sets, see the learned-orderer
+    profile) and the scores stay identical."""
+    import os
+
+    w = np.fromfile(os.path.join(os.path.dirname(gpu.__file__), "data", "orderer.f32"),
+                    dtype=np.float32)
+    q, r = gpu.generate(4, 2048, 16, 16)
+    s0, _, _, st0, _ = gpu.solve(q, r, 16, use_learned=0, tail_split_positions=-1)
+    gpu.mlp_load(w)
+    try:
+        s1, _, _, st1, _ = gpu.solve(q, r, 16, use_learned=1, tail_split_positions=-1)
+    finally:
+        gpu.mlp_load(None)
+    assert np.array_equal(s0, s1)
+    print("nodes: fastest-first %d, shipped weights %d (%.3f)" %
+          (st0.nodes, st1.nodes, st1.nodes / st0.nodes))
+    assert st1.nodes < 0.95 * st0.nodes
+
