@@ -102,13 +102,15 @@ typedef struct gpo_options {
 } gpo_options;
 
 typedef struct gpo_stats {
-  uint64_t nodes;          /* positions visited (root, children, pass frames) */
+  uint64_t nodes;          /* positions visited (root, children, pass frames; with a tail
+                              handoff, the stopped searches' nodes too) */
   uint64_t table_probes;   /* transposition-table lookups */
   uint64_t table_hits;     /* lookups that found the position */
   uint64_t table_updates;  /* stores into the table */
-  uint64_t learned_calls;  /* learned-orderer evaluations */
+  uint64_t learned_calls;  /* positions scored by the learned orderer */
   uint64_t splits;         /* moves of split nodes searched by helper lanes */
-  double kernel_ms;        /* device time of the search kernel (CUDA events) */
+  double kernel_ms;        /* device time of the search kernel (CUDA events; with a root
+                              split or a tail handoff, of every search launch) */
   double total_ms;         /* wall time of the call */
   uint64_t launches;       /* kernels the call launched */
   uint64_t stability_cuts; /* nodes closed by the stability cutoff */
